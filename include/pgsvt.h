@@ -1,0 +1,190 @@
+/*
+ * pgsvt.h — C ABI of the GB300 PGURE-SVT denoiser (libpgsvt.so).
+ *
+ * This is the drop-in boundary for the reference's denoising entry point
+ *
+ *   template <typename T1, typename T2>
+ *   uint32_t PGURESVT(arma::Cube<T2>& Y, arma::Mat<T2>& estimates,
+ *                     const arma::Cube<T1>& X, uint32_t trajLength,
+ *                     uint32_t blockSize, uint32_t blockOverlap,
+ *                     uint32_t motionWindow, int64_t medianSize,
+ *                     uint32_t noiseMethod, uint32_t maxIter, int64_t nJobs,
+ *                     int64_t randomSeed, bool optimizePGURE, bool expWeighting,
+ *                     bool motionEstimation, double lambdaEst, double alphaEst,
+ *                     double muEst, double sigmaEst, double tol, bool verbose)
+ *     (src/pguresvt.hpp:17-38; bound from Python in pguresvt/_pguresvt.pyx:143-148)
+ *
+ * Plain pointers and sizes only: no Armadillo, no torch types.  All arrays are
+ * column-major exactly like the reference's Armadillo cubes: element
+ * (r, c, t) of an nrows x ncols x nframes cube sits at r + c*nrows + t*nrows*ncols.
+ * `estimates` is the reference's Mat<double>(nframes, 4): element (t, j) at
+ * t + j*nframes, columns (lambda, alpha, mu, sigma) as in pguresvt.hpp:150-153.
+ *
+ * Every call computes on one CUDA device (the current one) with hand-written
+ * sm_103a kernels.  There is no CPU fallback: if no device is usable the call
+ * fails with PGSVT_ERR_CUDA.
+ */
+#ifndef PGSVT_H
+#define PGSVT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGSVT_ABI_VERSION 1
+
+/* Input element types: the reference instantiates PGURESVT for uint8, uint16,
+ * float and double inputs (pguresvt/_pguresvt.pyx:151,210,269,328). */
+typedef enum {
+  PGSVT_U8 = 0,
+  PGSVT_U16 = 1,
+  PGSVT_F32 = 2,
+  PGSVT_F64 = 3
+} pgsvt_dtype;
+
+typedef enum {
+  PGSVT_OK = 0,
+  PGSVT_ERR_INVALID_ARG = 1,   /* bad size / parameter (message says which) */
+  PGSVT_ERR_UNSUPPORTED = 2,   /* a reference feature this build does not run */
+  PGSVT_ERR_CUDA = 3,          /* CUDA runtime error or no usable device */
+  PGSVT_ERR_OOM = 4,           /* device allocation failed */
+  PGSVT_ERR_TIMEOUT = 5,       /* a bounded device wait expired */
+  PGSVT_ERR_NONFINITE = 6      /* input holds NaN / Inf */
+} pgsvt_status_code;
+
+/* Reference behaviours that are reproduced by default (parity mode).  Clearing
+ * a bit selects the evidently intended behaviour instead.                     */
+/* PGURE(u,p,alpha,sigma,mu,...) binds to the ctor's (alpha,mu,sigma): inside the
+ * risk mu and sigma are swapped (pguresvt.hpp:133 vs pgure.hpp:26-30).         */
+#define PGSVT_COMPAT_SWAP_MU_SIGMA 0x1u
+/* With motion estimation off, frames other than the reference frame keep
+ * trajectory coordinates (0,0) (arps.hpp:42,60-64).  Cleared: every frame uses
+ * the patch's own grid position.                                               */
+#define PGSVT_COMPAT_ZERO_MOTION 0x2u
+/* delta1 is an integer cube, so delta1*eps1 truncates eps1 to 0 and U1 == U
+ * (pgure.hpp:80,167-183): the first-order divergence term vanishes.  Cleared:
+ * U1 = U + eps1*delta1 is decomposed and the term is evaluated.               */
+#define PGSVT_COMPAT_INT_DELTA1 0x4u
+#define PGSVT_COMPAT_ALL 0x7u
+
+/* Parameters of PGURESVT (pguresvt.hpp:17-38), same names and sentinels:
+ * negative lambda/alpha/mu/sigma mean "estimate", random_seed < 0 seeds from
+ * std::random_device, median_size <= 0 disables the median pre-filter.      */
+typedef struct {
+  uint32_t traj_length;     /* trajLength   (Python: trajectory_length) */
+  uint32_t block_size;      /* blockSize    (patch_size)                */
+  uint32_t block_overlap;   /* blockOverlap (patch_overlap)             */
+  uint32_t motion_window;   /* motionWindow (motion_window)             */
+  int64_t median_size;      /* medianSize   (motion_filter)             */
+  uint32_t noise_method;    /* noiseMethod  (noise_method)              */
+  uint32_t max_iter;        /* maxIter: cap on risk evaluations/window  */
+  int64_t n_jobs;           /* nJobs: host threads (staging only)       */
+  int64_t random_seed;      /* randomSeed                               */
+  int32_t optimize_pgure;   /* optimizePGURE                            */
+  int32_t exp_weighting;    /* expWeighting                             */
+  int32_t motion_estimation;/* motionEstimation                         */
+  int32_t verbose;          /* verbose                                  */
+  double lambda;            /* lambdaEst (start point when optimising)  */
+  double alpha;             /* alphaEst                                 */
+  double mu;                /* muEst                                    */
+  double sigma;             /* sigmaEst                                 */
+  double tol;               /* tol (ftol of the lambda search)          */
+  uint32_t compat_flags;    /* PGSVT_COMPAT_* (default PGSVT_COMPAT_ALL)*/
+  uint32_t search_points;   /* lambda values per search round (0: 8)    */
+  uint32_t search_rounds;   /* refinement rounds after the grid (0: 4)  */
+  uint32_t window_batch;    /* windows in flight on the device (0: auto)*/
+  double lambda_hint;       /* >0: narrow search around this proposal   */
+  double hint_span;         /* bracket [hint/span, hint*span] (0: 2.0)  */
+} pgsvt_params;
+
+/* Per-call report.  All times are wall seconds measured by the library. */
+typedef struct {
+  int32_t code;             /* pgsvt_status_code of the call              */
+  int32_t cuda_error;       /* last cudaError_t seen (0 if none)          */
+  uint64_t windows;         /* windows (output frames) processed          */
+  uint64_t risk_evals;      /* lambda values evaluated over all windows   */
+  uint64_t kernel_launches; /* kernels launched by the call               */
+  uint64_t h2d_bytes;       /* host->device bytes copied                  */
+  uint64_t d2h_bytes;       /* device->host bytes copied                  */
+  double seconds;           /* whole call                                 */
+  char message[256];        /* human-readable error / note                */
+} pgsvt_status;
+
+/* Fill *p with the reference defaults (pguresvt/_pguresvt.pyx:151-168 and
+ * pguresvt/svt.py:172-191): T=15, patch 4, overlap 1, motion window 7,
+ * median 5, noise method 4, max_iter 500, n_jobs -1, seed -1, optimise,
+ * exponential weighting, motion estimation on, lambda/alpha/mu/sigma -1,
+ * tol 1e-7, compat PGSVT_COMPAT_ALL.                                       */
+int pgsvt_default_params(pgsvt_params* p);
+
+/* Denoise an image sequence: the replacement for PGURESVT<T1,double>
+ * (pguresvt.hpp:17-172).  X is host memory (nrows x ncols x nframes, dtype
+ * `dtype`), Y (same shape, double) and estimates (nframes x 4, double) are
+ * host memory owned by the caller.  Returns a pgsvt_status_code; `st` may be
+ * NULL.  Frames must be square (the reference's ARPS indexing assumes it,
+ * arps.hpp:186-187) and nframes >= the clamped trajectory length.          */
+int pgsvt_denoise(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                  uint32_t nframes, double* Y, double* estimates,
+                  const pgsvt_params* p, pgsvt_status* st);
+
+/* Same as pgsvt_denoise with X, Y, estimates already in device memory of the
+ * current device; `stream` is a cudaStream_t (NULL: the library's stream).
+ * The call returns after the work has completed.                          */
+int pgsvt_denoise_device(const void* X_dev, int32_t dtype, uint32_t nrows,
+                         uint32_t ncols, uint32_t nframes, double* Y_dev,
+                         double* estimates_dev, const pgsvt_params* p,
+                         void* stream, pgsvt_status* st);
+
+/* --- Component entry points (one reference stage each, host buffers) --- */
+
+/* ARPS block matching for one window (MotionEstimator::Estimate,
+ * arps.hpp:52-134).  `w` is the max-normalised window (double, nrows x nrows
+ * x nwin with nwin = 2*(T/2)+1); time_iter / frame_window / nimages are the
+ * reference's timeIter / timeWindow / nImages.  Writes the trajectory table
+ * (the reference's icube patches(2, P, nwin)) as rows[k*P+it], cols[k*P+it].*/
+int pgsvt_arps_window(const double* w, uint32_t nrows, uint32_t nwin,
+                      uint32_t block_size, uint32_t motion_window,
+                      uint32_t time_iter, uint32_t frame_window,
+                      uint32_t nimages, int32_t motion_estimation,
+                      uint32_t compat_flags, int32_t* rows, int32_t* cols);
+
+/* Singular values of every kept patch's Casorati matrix for one window
+ * (SVT::Decompose, svt.hpp:58-118).  `u` is the normalised window, rows/cols
+ * the trajectory table.  S is npatch x nwin (descending per patch);
+ * *npatch receives the number of kept patches (svt.hpp:61-94).            */
+int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin,
+                     uint32_t block_size, uint32_t block_overlap,
+                     const int32_t* rows, const int32_t* cols, float* S,
+                     uint32_t* npatch);
+
+/* Singular-value thresholding reconstruction of one window at `lambda`
+ * (SVT::Reconstruct, svt.hpp:121-167): v is nrows x nrows x nwin double. */
+int pgsvt_reconstruct_window(const double* u, uint32_t nrows, uint32_t nwin,
+                             uint32_t block_size, uint32_t block_overlap,
+                             int32_t exp_weighting, const int32_t* rows,
+                             const int32_t* cols, double lambda, double* v);
+
+/* PGURE risk of one window at `nl` lambda values (PGURE ctor + CalculatePGURE,
+ * pgure.hpp:26-137).  alpha/mu/sigma are the caller-side values passed to
+ * PGURE (the swap of PGSVT_COMPAT_SWAP_MU_SIGMA is applied inside).         */
+int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin,
+                      uint32_t block_size, uint32_t block_overlap,
+                      int32_t exp_weighting, const int32_t* rows,
+                      const int32_t* cols, double alpha, double mu,
+                      double sigma, int64_t random_seed, uint32_t compat_flags,
+                      const double* lambdas, uint32_t nl, double* risk);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* pgsvt_last_error(void);
+
+/* Library version string, e.g. "pgsvt-gb300 0.1.0 (sm_103a)". */
+const char* pgsvt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PGSVT_H */

@@ -1,0 +1,93 @@
+/*
+ * pgsvt_oracle.h — C API of the CPU oracle (test infrastructure only).
+ *
+ * The oracle is an FP64 restatement of the reference's denoising path
+ * (src/pguresvt.hpp, src/arps.hpp, src/svt.hpp, src/pgure.hpp,
+ * src/utils.hpp of tjof2/pgure-svt 0.6.4).  It is the parity checker for the
+ * CUDA library and the timed CPU baseline; nothing in the product links it.
+ * The SVD is LAPACK dgesdd (the routine behind arma::svd_econ's default "dc"
+ * method), supplied at run time as a function pointer (orc_set_dgesdd).
+ */
+#ifndef PGSVT_ORACLE_H
+#define PGSVT_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void (*orc_dgesdd_fn)(char* jobz, int* m, int* n, double* a, int* lda,
+                              double* s, double* u, int* ldu, double* vt,
+                              int* ldvt, double* work, int* lwork, int* iwork,
+                              int* info);
+
+/* Same fields, order and meaning as pgsvt_params (include/pgsvt.h). */
+typedef struct {
+  uint32_t traj_length, block_size, block_overlap, motion_window;
+  int64_t median_size;
+  uint32_t noise_method, max_iter;
+  int64_t n_jobs, random_seed;
+  int32_t optimize_pgure, exp_weighting, motion_estimation, verbose;
+  double lambda, alpha, mu, sigma, tol;
+  uint32_t compat_flags, search_points, search_rounds, window_batch;
+  double lambda_hint, hint_span;
+} orc_params;
+
+typedef struct {
+  uint64_t windows;
+  uint64_t risk_evals;
+  double seconds;
+} orc_report;
+
+void orc_set_dgesdd(orc_dgesdd_fn fn);
+
+/* PGURE probes (pgure.hpp:167-186): delta1 (+-1) then delta2, n each. */
+int orc_probes(int64_t seed, uint64_t n, int8_t* d1, double* d2);
+
+/* Kept patch indices (svt.hpp:61-94), sorted unique.  out may be NULL to
+ * query the count only. */
+int orc_patch_list(uint32_t side, uint32_t bs, uint32_t ov, int64_t* out,
+                   uint64_t* count);
+
+int orc_arps_window(const double* w, uint32_t side, uint32_t nwin, uint32_t bs,
+                    uint32_t mw, uint32_t time_iter, uint32_t frame_window,
+                    uint32_t nimages, int32_t motion, uint32_t compat,
+                    int32_t* rows, int32_t* cols);
+
+int orc_svd_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs,
+                   uint32_t ov, const int32_t* rows, const int32_t* cols,
+                   double* S, uint64_t* npatch);
+
+int orc_reconstruct_window(const double* u, uint32_t side, uint32_t nwin,
+                           uint32_t bs, uint32_t ov, int32_t expw,
+                           const int32_t* rows, const int32_t* cols,
+                           double lambda, double* v);
+
+int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs,
+                    uint32_t ov, int32_t expw, const int32_t* rows,
+                    const int32_t* cols, double alpha, double mu, double sigma,
+                    int64_t seed, uint32_t compat, const double* lambdas,
+                    uint32_t nl, double* risk);
+
+/* Whole sequence (PGURESVT<T1,double>, pguresvt.hpp:17-172); X is FP64. */
+int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols,
+                uint32_t nimages, const orc_params* p, double* Y,
+                double* estimates, orc_report* rep);
+
+/* Timing sample for the CPU baseline: runs the per-window pipeline of
+ * `nwindows` windows (starting at window `first`) on `threads` threads with
+ * only every `stride`-th patch position kept in ARPS / SVD / reconstruction
+ * and a fixed number of risk evaluations per window (`evals`).  Returns the
+ * wall seconds in *seconds. */
+int orc_time_sample(const double* X, uint32_t nrows, uint32_t nimages,
+                    const orc_params* p, uint32_t first, uint32_t nwindows,
+                    uint32_t threads, uint32_t stride, uint32_t evals,
+                    double* seconds);
+
+const char* orc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,284 @@
+// arps.cu — ARPS block matching on the GPU with motion vectors identical to
+// the reference's FP64 MotionEstimator (arps.hpp:52-375).
+//
+// One thread runs one motion-slot chain (<= 2 frame pairs that share a slot of
+// the reference's `motions` cube, arps.hpp:121-130) for one grid position.
+// Block costs (mean squared difference, arps.hpp:148-151) are computed in FP32
+// from the normalised window together with a rigorous bound on their distance
+// to the FP64 value; whenever the FP32 argmin of a diamond step is not certain
+// under those bounds, every candidate of that step is recomputed exactly as the
+// reference does (FP64 x/umax, FP64 squares, Armadillo's two-accumulator
+// accu(), no fused multiply-add) and the FP64 argmin is taken.  The decisions,
+// hence the motion vectors, are therefore the FP64 ones.
+#include "pgsvt_internal.h"
+
+namespace pgsvt {
+
+namespace {
+
+
+struct ArpsCtx {
+  const float* fa1;   // normalised window slice a1
+  const float* fa2;   // normalised window slice a2
+  const float* xa1;   // input frames (exact f32 values) for the FP64 path
+  const float* xa2;
+  const double* xa1d; // input frames when the input is f64
+  const double* xa2d;
+  double umax;
+  int S;
+  int mw;
+};
+
+template <int BS>
+struct Block {
+  float ref[BS * BS];
+
+  __device__ void load(const ArpsCtx& c, int i, int j) {
+#pragma unroll
+    for (int cc = 0; cc < BS; ++cc)
+#pragma unroll
+      for (int r = 0; r < BS; ++r) ref[r + cc * BS] = __ldg(c.fa1 + (i + r) + (size_t)(j + cc) * c.S);
+  }
+
+  // FP32 cost and a bound on |cost32 - cost64|:
+  //   2^-24 * (24 * sum_e (|a_e|+|b_e|)^2 / m + 2 * cost)
+  __device__ void cost32(const ArpsCtx& c, int y, int x, float& cost, float& err) const {
+    float acc = 0.f, sb = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < BS; ++cc)
+#pragma unroll
+      for (int r = 0; r < BS; ++r) {
+        const float a = ref[r + cc * BS];
+        const float b = __ldg(c.fa2 + (y + r) + (size_t)(x + cc) * c.S);
+        const float d = a - b;
+        acc = fmaf(d, d, acc);
+        const float s = fabsf(a) + fabsf(b);
+        sb = fmaf(s, s, sb);
+      }
+    const float oo = 1.0f / (float)(BS * BS);
+    cost = acc * oo;
+    err = 5.9604645e-8f * (24.f * sb * oo + 2.f * cost);
+  }
+};
+
+__device__ __forceinline__ double src64(const ArpsCtx& c, const float* xf, const double* xd,
+                                        size_t idx) {
+  return xd ? xd[idx] : (double)xf[idx];
+}
+
+// Exact reference cost between the block at (i,j) of slice a1 and (y,x) of a2.
+template <int BS>
+__device__ double cost64(const ArpsCtx& c, int i, int j, int y, int x) {
+  double v1 = 0.0, v2 = 0.0;
+  const double oo = 1.0 / (double)(BS * BS);
+#pragma unroll
+  for (int e = 0; e < BS * BS; ++e) {
+    const int r = e % BS, cc = e / BS;
+    const double a = __ddiv_rn(src64(c, c.xa1, c.xa1d, (i + r) + (size_t)(j + cc) * c.S), c.umax);
+    const double b = __ddiv_rn(src64(c, c.xa2, c.xa2d, (y + r) + (size_t)(x + cc) * c.S), c.umax);
+    const double d = __dsub_rn(a, b);
+    const double sq = __dmul_rn(d, d);
+    if (e & 1) v2 = __dadd_rn(v2, sq);
+    else v1 = __dadd_rn(v1, sq);
+  }
+  return __dmul_rn(__dadd_rn(v1, v2), oo);
+}
+
+// First index of the minimum among evaluated slots; recomputes in FP64 when
+// the FP32 decision is not certain.  off[k] = (dx, dy) relative to (y, x).
+template <int BS>
+__device__ int pick(const ArpsCtx& c, const float* cs, const float* es, const bool* ev,
+                    const int (*off)[2], int nslot, int i, int j, int y, int x,
+                    unsigned long long* nexact) {
+  int ks = 2;
+  float best = cs[2];
+  for (int k = 0; k < nslot; ++k)
+    if (ev[k] && (cs[k] < best || (cs[k] == best && k < ks))) {
+      best = cs[k];
+      ks = k;
+    }
+  bool certain = true;
+  const float hi = cs[ks] + es[ks];
+  for (int k = 0; k < nslot; ++k) {
+    if (!ev[k] || k == ks) continue;
+    const float lo = cs[k] - es[k];
+    if (k < ks ? !(lo > hi) : !(lo >= hi)) certain = false;
+  }
+  if (certain) return ks;
+  atomicAdd(nexact, 1ull);
+  double c64[6];
+  for (int k = 0; k < nslot; ++k)
+    c64[k] = ev[k] ? cost64<BS>(c, i, j, y + off[k][1], x + off[k][0]) : 1e9;
+  double m = c64[0];
+  for (int k = 1; k < nslot; ++k) m = fmin(m, c64[k]);
+  for (int k = 0; k < nslot; ++k)
+    if (c64[k] == m) return k;
+  return 2;
+}
+
+// ARPSMotionEstimation (arps.hpp:153-375) for one position of one frame pair.
+// (my, mx) holds the predictor slot on entry and the new motion on exit.
+template <int BS>
+__device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, int& ox,
+                          unsigned long long* nexact) {
+  const int S = c.S, M = c.mw, Wd = 2 * M + 1;
+  const int n1 = S - BS + 1;
+  const int i = it % n1, j = it / n1;
+  Block<BS> blk;
+  blk.load(c, i, j);
+  uint32_t seen[(2 * kMaxMW + 1) * (2 * kMaxMW + 1) / 32 + 1];
+  const int nw = (Wd * Wd + 31) / 32;
+  for (int q = 0; q < nw; ++q) seen[q] = 0u;
+  auto mark = [&](int dy, int dx) {
+    if (dy < -M || dy > M || dx < -M || dx > M) return;  // cannot occur for mw >= 2
+    const int b = (dy + M) * Wd + (dx + M);
+    seen[b >> 5] |= 1u << (b & 31);
+  };
+  auto is_seen = [&](int dy, int dx) {
+    const int b = (dy + M) * Wd + (dx + M);
+    return (seen[b >> 5] >> (b & 31)) & 1u;
+  };
+  int x = j, y = i;
+  float cs[6], es[6];
+  bool ev[6];
+  float curC, curE;
+  blk.cost32(c, i, j, curC, curE);
+  mark(0, 0);
+  int step, nld;
+  int LD[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  if (j == 0) {
+    step = 2;
+    nld = 5;
+  } else {
+    const int ay = abs(my), ax = abs(mx);
+    step = (ax <= ay) ? ay : ax;
+    if ((ay == 0 && ax == step) || (ax == 0 && ay == step)) {
+      nld = 5;
+    } else {
+      nld = 6;
+      LD[5][0] = mx;
+      LD[5][1] = my;
+    }
+  }
+  LD[0][1] = -step;
+  LD[1][0] = -step;
+  LD[3][0] = step;
+  LD[4][1] = step;
+  // LDSP (arps.hpp:247-294)
+  for (int k = 0; k < 6; ++k) ev[k] = false;
+  ev[2] = true;
+  cs[2] = curC;
+  es[2] = curE;
+  for (int k = 0; k < nld; ++k) {
+    if (k == 2 || step == 0) continue;
+    const int vy = y + LD[k][1], hx = x + LD[k][0];
+    if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
+    blk.cost32(c, vy, hx, cs[k], es[k]);
+    ev[k] = true;
+    mark(LD[k][1], LD[k][0]);
+  }
+  int ks = pick<BS>(c, cs, es, ev, LD, 6, i, j, y, x, nexact);
+  x += LD[ks][0];
+  y += LD[ks][1];
+  curC = cs[ks];
+  curE = es[ks];
+  // SDSP (arps.hpp:299-368); every move enters an unvisited cell, so the loop
+  // ends within Wd*Wd iterations.
+  const int SD[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
+  for (int n = 0; n < Wd * Wd + 1; ++n) {
+    for (int k = 0; k < 6; ++k) ev[k] = false;
+    ev[2] = true;
+    cs[2] = curC;
+    es[2] = curE;
+    for (int k = 0; k < 5; ++k) {
+      if (k == 2) continue;
+      const int vy = y + SD[k][1], hx = x + SD[k][0];
+      if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
+      if (hx < j - M || hx > j + M || vy < i - M || vy > i + M) continue;
+      if (is_seen(vy - i, hx - j)) continue;
+      blk.cost32(c, vy, hx, cs[k], es[k]);
+      ev[k] = true;
+      mark(vy - i, hx - j);
+    }
+    ks = pick<BS>(c, cs, es, ev, SD, 5, i, j, y, x, nexact);
+    if (ks == 2) break;
+    x += SD[ks][0];
+    y += SD[ks][1];
+    curC = cs[ks];
+    curE = es[ks];
+  }
+  my = y - i;
+  mx = x - j;
+  oy = y;
+  ox = x;
+}
+
+template <int BS>
+__global__ void k_arps(Problem pb, DeviceBuffers d) {
+  const Geometry& g = pb.g;
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ch = blockIdx.y, w = blockIdx.z;
+  if (it >= g.P) return;
+  const ArpsChain cn = d.chains[w * d.nchains + ch];
+  if (cn.npairs == 0) return;
+  const WinConst& wc = d.wc[w];
+  const size_t F = g.F();
+  ArpsCtx c;
+  c.umax = wc.unorm;
+  c.S = g.S;
+  c.mw = g.mw;
+  int my = 0, mx = 0;
+  for (int q = 0; q < cn.npairs; ++q) {
+    const int a1 = cn.a1[q], a2 = cn.a2[q];
+    c.fa1 = d.u + ((size_t)w * g.nwin + a1) * F;
+    c.fa2 = d.u + ((size_t)w * g.nwin + a2) * F;
+    c.xa1 = d.xs + (size_t)(wc.s0 + a1) * F;
+    c.xa2 = d.xs + (size_t)(wc.s0 + a2) * F;
+    c.xa1d = d.x64 ? d.x64 + (size_t)(wc.s0 + a1) * F : nullptr;
+    c.xa2d = d.x64 ? d.x64 + (size_t)(wc.s0 + a2) * F : nullptr;
+    int oy, ox;
+    arps_pair<BS>(c, it, my, mx, oy, ox, d.counters);
+    d.pos[((size_t)w * g.nwin + a2) * g.P + it] = (uint32_t)oy | ((uint32_t)ox << 16);
+  }
+}
+
+// Reference slice (always) and, without motion estimation, the other slices:
+// (0,0) in compat mode (arps.hpp:42), else the grid position.
+__global__ void k_grid(Problem pb, DeviceBuffers d) {
+  const Geometry& g = pb.g;
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y, w = blockIdx.z;
+  if (it >= g.P) return;
+  const int ref = d.wc[w].ref;
+  const int n1 = g.S - g.bs + 1;
+  const uint32_t grid = (uint32_t)(it % n1) | ((uint32_t)(it / n1) << 16);
+  uint32_t v;
+  if (k == ref) v = grid;
+  else if (pb.motion) return;  // written by k_arps
+  else v = (pb.compat & 0x2) ? 0u : grid;
+  d.pos[((size_t)w * g.nwin + k) * g.P + it] = v;
+}
+
+}  // namespace
+
+cudaError_t launch_arps(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+  const Geometry& g = pb.g;
+  const int threads = 128;
+  dim3 gg((g.P + threads - 1) / threads, g.nwin, pb.W);
+  k_grid<<<gg, threads, 0, s>>>(pb, d);
+  if (!pb.motion || d.nchains == 0) return cudaGetLastError();
+  dim3 ga((g.P + threads - 1) / threads, d.nchains, pb.W);
+  switch (g.bs) {
+    case 2: k_arps<2><<<ga, threads, 0, s>>>(pb, d); break;
+    case 3: k_arps<3><<<ga, threads, 0, s>>>(pb, d); break;
+    case 4: k_arps<4><<<ga, threads, 0, s>>>(pb, d); break;
+    case 5: k_arps<5><<<ga, threads, 0, s>>>(pb, d); break;
+    case 6: k_arps<6><<<ga, threads, 0, s>>>(pb, d); break;
+    case 7: k_arps<7><<<ga, threads, 0, s>>>(pb, d); break;
+    case 8: k_arps<8><<<ga, threads, 0, s>>>(pb, d); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace pgsvt

@@ -1,0 +1,786 @@
+// capi.cu — host orchestration and the C ABI of libpgsvt (include/pgsvt.h).
+//
+// pgsvt_denoise replaces PGURESVT<T1,double> (pguresvt.hpp:17-172).  Instead of
+// the reference's std::thread fan-out over output frames (utils.hpp:108-168),
+// windows are processed W at a time on one device: every kernel of the
+// per-window pipeline runs over the whole batch, and the lambda search is a
+// device-resident state machine, so a batch is one fixed, synchronisation-free
+// launch sequence on one stream.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pgsvt.h"
+#include "pgsvt_internal.h"
+
+using namespace pgsvt;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Fail : std::runtime_error {
+  int code;
+  int cuda;
+  Fail(int c, const std::string& m, int ce = 0) : std::runtime_error(m), code(c), cuda(ce) {}
+};
+
+#define PGSVT_CK(x)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess)                                                           \
+      throw Fail(e_ == cudaErrorMemoryAllocation ? PGSVT_ERR_OOM : PGSVT_ERR_CUDA,   \
+                 std::string(#x) + ": " + cudaGetErrorString(e_), (int)e_);          \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Probes: pcg64 (O'Neill's PCG, 128-bit LCG with XSL-RR output, seeded as the
+// reference's RNG.seed(randomSeed), pgure.hpp:52-59) feeding
+// std::bernoulli_distribution semantics (one 64-bit draw scaled by 2^-64,
+// true when below p), in column-major cube order, delta1 then delta2
+// (pgure.hpp:167-186).
+class Pcg64 {
+ public:
+  using u128 = unsigned __int128;
+  explicit Pcg64(u128 seed) {
+    inc_ = ((u128)6364136223846793005ULL << 64) | 1442695040888963407ULL;
+    state_ = (seed + inc_) * mult() + inc_;
+  }
+  uint64_t operator()() {
+    state_ = state_ * mult() + inc_;
+    const uint64_t hi = (uint64_t)(state_ >> 64), lo = (uint64_t)state_;
+    const unsigned rot = (unsigned)(hi >> 58);
+    const uint64_t x = hi ^ lo;
+    return (x >> rot) | (x << ((64u - rot) & 63u));
+  }
+
+ private:
+  static u128 mult() { return ((u128)2549297995355413924ULL << 64) | 4865540595714422341ULL; }
+  u128 state_, inc_;
+};
+
+bool draw(Pcg64& g, double p) {
+  double u = (double)g() / 18446744073709551616.0;
+  if (u >= 1.0) u = std::nextafter(1.0, 0.0);
+  return u < p;
+}
+
+double probe_vp() {
+  const double kappa = 1.0;
+  return 0.5 + 0.5 * kappa / std::sqrt(kappa * kappa + 4);
+}
+
+void make_probes(int64_t seed, size_t n, int8_t* d1, int8_t* d2code) {
+  Pcg64::u128 s;
+  if (seed >= 0) {
+    s = (Pcg64::u128)(uint64_t)seed;
+  } else {
+    std::random_device rd;
+    s = ((Pcg64::u128)(((uint64_t)rd() << 32) | rd()) << 64) | (((uint64_t)rd() << 32) | rd());
+  }
+  Pcg64 g(s);
+  const double vP = probe_vp();
+  for (size_t i = 0; i < n; ++i) d1[i] = draw(g, 0.5) ? -1 : 1;
+  for (size_t i = 0; i < n; ++i) d2code[i] = draw(g, vP) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Kept patches (svt.hpp:61-94): the row-major-looking index i*nyMbs + j of the
+// first loop is reproduced as written, then the right and bottom edges are
+// added and the set is sorted and made unique.
+std::vector<int32_t> patch_list(int S, int bs, int ov) {
+  const int64_t nMbs = S - bs;
+  std::vector<int64_t> v;
+  for (int64_t i = 0; i < 1 + nMbs; i += ov)
+    for (int64_t j = 0; j < 1 + nMbs; j += ov) v.push_back(i * nMbs + j);
+  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * i + nMbs);
+  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * nMbs + i);
+  std::sort(v.begin(), v.end());
+  v.erase(std::unique(v.begin(), v.end()), v.end());
+  return std::vector<int32_t>(v.begin(), v.end());
+}
+
+// Frame pairs of MotionEstimator::Estimate (arps.hpp:52-134) grouped into
+// chains of pairs that share a motion slot (the only data dependence).
+std::vector<ArpsChain> chains_for(int t, int tw, int nimg, int nwin) {
+  struct Pr { int a1, a2, a3; };
+  std::vector<Pr> prs;
+  if (t < tw) {
+    const int loopEnd = nwin - t - 1;
+    for (int i = 0; i < loopEnd; ++i) prs.push_back({t + i, t + i + 1, t + i});
+    for (int i = 0; i < t; ++i) prs.push_back({t - i, t - i - 1, t - i});
+  } else if (t >= nimg - tw) {
+    const int e = t - (nimg - nwin), loopEnd = 2 * tw - e;
+    for (int i = 0; i < loopEnd; ++i) prs.push_back({e + i, e + i + 1, e + i});
+    for (int i = 0; i < e; ++i) {
+      if (2 * tw == e) prs.push_back({e - i, e - i - 1, e - i - 1});
+      else prs.push_back({e - i, e - i - 1, e - i});
+    }
+  } else {
+    for (int i = 0; i < tw; ++i) prs.push_back({tw + i, tw + i + 1, tw + i});
+    for (int i = 0; i < tw; ++i) prs.push_back({tw - i, tw - i - 1, tw - i});
+  }
+  std::vector<ArpsChain> out(2 * tw);
+  std::vector<int> slot_of(2 * tw + 1, -1);
+  int n = 0;
+  for (const Pr& p : prs) {
+    int& c = slot_of[p.a3];
+    if (c < 0) c = n++;
+    ArpsChain& ch = out[c];
+    if (ch.npairs >= 2) throw Fail(PGSVT_ERR_INVALID_ARG, "ARPS chain longer than 2 pairs");
+    ch.a1[ch.npairs] = (int8_t)p.a1;
+    ch.a2[ch.npairs] = (int8_t)p.a2;
+    ch.npairs++;
+  }
+  return out;
+}
+
+struct DevMem {
+  std::vector<void*> ptrs;
+  void* get(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    PGSVT_CK(cudaMalloc(&p, bytes));
+    ptrs.push_back(p);
+    return p;
+  }
+  template <typename T>
+  T* arr(size_t n) { return (T*)get(n * sizeof(T)); }
+  ~DevMem() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
+struct Stats {
+  uint64_t launches = 0, h2d = 0, d2h = 0, evals = 0;
+};
+
+void check_launch(cudaError_t e, Stats& s, int n = 1) {
+  s.launches += n;
+  PGSVT_CK(e);
+}
+
+// Validation mirroring pguresvt/svt.py:212-271 and the limits of this build.
+void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
+  if (nr == 0 || nc == 0 || nimg == 0) throw Fail(PGSVT_ERR_INVALID_ARG, "empty input");
+  if (nr != nc)
+    throw Fail(PGSVT_ERR_INVALID_ARG, "frames must be square (the reference's ARPS indexing, "
+                                      "arps.hpp:186-187, assumes nrows == ncols)");
+  if (nr > 32767) throw Fail(PGSVT_ERR_UNSUPPORTED, "frame side above 32767");
+  if (p.block_size < 2 || p.block_size > 8)
+    throw Fail(PGSVT_ERR_UNSUPPORTED, "block_size must be in [2, 8] in this build");
+  if (p.block_size > nr) throw Fail(PGSVT_ERR_INVALID_ARG, "block_size larger than the frame");
+  if (p.block_overlap < 1 || p.block_overlap > p.block_size)
+    throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid patch_overlap parameter: must be in [1, block_size]");
+  if (p.traj_length < 1) throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid trajectory_length parameter");
+  const uint32_t Ntc = (p.block_size * p.block_size < p.traj_length)
+                           ? p.block_size * p.block_size - 1 : p.traj_length;
+  const uint32_t nwin = 2 * (Ntc / 2) + 1;
+  if (nimg < nwin) throw Fail(PGSVT_ERR_INVALID_ARG, "sequence shorter than the trajectory");
+  if (!svd_supported((int)p.block_size, (int)nwin))
+    throw Fail(PGSVT_ERR_UNSUPPORTED, "trajectory window above 21 frames in this build");
+  if (p.motion_estimation && (p.motion_window < 2 || p.motion_window > (uint32_t)kMaxMW))
+    throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid motion_window parameter: must be in [2, 15]");
+  if (p.median_size > 0)
+    throw Fail(PGSVT_ERR_UNSUPPORTED, "median pre-filter (motion_filter) is not built; pass <= 0");
+  if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0))
+    throw Fail(PGSVT_ERR_UNSUPPORTED,
+               "noise estimation is not built: give noise alpha, mu and sigma (>= 0)");
+  if (!p.optimize_pgure && !(p.lambda >= 0))
+    throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid lambda1 parameter: must be >= 0 without optimisation");
+  if (p.search_points > (uint32_t)kMaxK)
+    throw Fail(PGSVT_ERR_INVALID_ARG, "search_points above 16");
+}
+
+struct Setup {
+  Geometry g;
+  int K, rounds, max_rounds;
+  std::vector<int32_t> plist;
+};
+
+Setup make_setup(const pgsvt_params& p, int S, int nimg) {
+  Setup s;
+  Geometry& g = s.g;
+  g.S = S;
+  g.bs = (int)p.block_size;
+  g.M = g.bs * g.bs;
+  g.Ntc = (g.M < (int)p.traj_length) ? g.M - 1 : (int)p.traj_length;  // pguresvt.hpp:57
+  g.fw = g.Ntc / 2;                                                   // pguresvt.hpp:58
+  g.nwin = 2 * g.fw + 1;
+  g.P = (S - g.bs + 1) * (S - g.bs + 1);
+  s.plist = patch_list(S, g.bs, (int)p.block_overlap);
+  g.NP = (int)s.plist.size();
+  g.NC = svd_columns(g.nwin);
+  g.mw = (int)p.motion_window;
+  g.nimg = nimg;
+  s.K = p.search_points ? (int)p.search_points : 8;
+  s.rounds = p.search_rounds ? (int)p.search_rounds : 4;
+  // bound the points a window keeps
+  while (s.K * (1 + s.rounds) > kMaxPts && s.rounds > 0) --s.rounds;
+  // plain: 1 grid + rounds refinements; hinted: 1 + rounds/2, then possibly plain again
+  s.max_rounds = p.lambda_hint > 0 ? (1 + std::max(1, s.rounds / 2)) + (1 + s.rounds)
+                                   : 1 + s.rounds;
+  return s;
+}
+
+Problem make_problem(const pgsvt_params& p, const Setup& su) {
+  Problem pb;
+  pb.g = su.g;
+  pb.W = 0;
+  pb.K = su.K;
+  pb.optimize = p.optimize_pgure ? 1 : 0;
+  pb.expw = p.exp_weighting ? 1 : 0;
+  pb.motion = p.motion_estimation ? 1 : 0;
+  pb.compat = (int)p.compat_flags;
+  pb.alpha_c = p.alpha;
+  pb.mu_c = p.mu;
+  pb.sigma_c = p.sigma;
+  pb.lambda_user = p.lambda;
+  pb.tol = p.tol;
+  pb.max_evals = std::max<int>(1, (int)p.max_iter);
+  pb.rounds = su.rounds;
+  pb.hint = p.lambda_hint;
+  pb.hint_span = p.hint_span > 1.0 ? p.hint_span : 2.0;
+  return pb;
+}
+
+// Bytes of device memory one window of a batch needs.
+size_t window_bytes(const Problem& pb, int ncopies) {
+  const Geometry& g = pb.g;
+  const size_t C = g.cube(), NP = g.NP, NC = g.NC;
+  size_t b = 0;
+  b += C * 4;                       // u
+  b += (size_t)g.nwin * g.P * 4;    // pos
+  b += C * 4;                       // cnt
+  b += C * 4 * 3;                   // fields
+  b += NC * g.M * NP * 4;           // U0
+  b += NC * g.nwin * NP * 4;        // V0
+  b += 2 * 4 * NC * NP * 4;         // sv, hv
+  b += (size_t)pb.K * C * 8;        // acc
+  b += (size_t)pb.K * ((NP + 31) / 32 + mse_blocks(g)) * 8 + 256 * 8;  // partials
+  b += sizeof(WinConst) + sizeof(SearchState) + 2 * (size_t)g.fw * sizeof(ArpsChain);
+  (void)ncopies;
+  return b;
+}
+
+// The per-sequence engine.  X_dev holds the input (dtype) on the device.
+void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, double* est_dev,
+                  const pgsvt_params& p, cudaStream_t s, Stats& stats) {
+  Setup su = make_setup(p, S, nimg);
+  Problem pb = make_problem(p, su);
+  const Geometry& g = pb.g;
+  DevMem mem;
+  const size_t F = g.F(), C = g.cube();
+  // sequence buffers
+  float* xs = mem.arr<float>((size_t)nimg * F);
+  double* x64 = (dtype == PGSVT_F64) ? mem.arr<double>((size_t)nimg * F) : nullptr;
+  double* fmx = mem.arr<double>(nimg);
+  check_launch(launch_convert(X_dev, dtype, (size_t)nimg * F, xs, x64, s), stats);
+  check_launch(launch_frame_max(xs, x64, nimg, F, fmx, s), stats);
+  std::vector<double> hmax(nimg);
+  PGSVT_CK(cudaMemcpyAsync(hmax.data(), fmx, sizeof(double) * nimg, cudaMemcpyDeviceToHost, s));
+  PGSVT_CK(cudaStreamSynchronize(s));
+  stats.d2h += sizeof(double) * nimg;
+  for (double v : hmax)
+    if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
+
+  const int ncopies = !pb.optimize ? 1 : ((pb.compat & PGSVT_COMPAT_INT_DELTA1) ? 3 : 4);
+  // batch size
+  size_t freeb = 0, totb = 0;
+  PGSVT_CK(cudaMemGetInfo(&freeb, &totb));
+  const size_t per = window_bytes(pb, ncopies);
+  const size_t budget = std::min<size_t>(freeb / 2, (size_t)48 << 30);
+  int W = p.window_batch ? (int)p.window_batch : (int)std::max<size_t>(1, budget / per);
+  W = std::max(1, std::min({W, nimg, 32}));
+  if ((size_t)W * per > freeb) throw Fail(PGSVT_ERR_OOM, "not enough device memory for one window");
+
+  // batch buffers
+  DeviceBuffers d{};
+  d.xs = xs;
+  d.x64 = x64;
+  d.fmax = fmx;
+  d.u = mem.arr<float>((size_t)W * C);
+  d.pos = mem.arr<uint32_t>((size_t)W * g.nwin * g.P);
+  int32_t* plist = mem.arr<int32_t>(g.NP);
+  PGSVT_CK(cudaMemcpyAsync(plist, su.plist.data(), sizeof(int32_t) * g.NP, cudaMemcpyHostToDevice, s));
+  stats.h2d += sizeof(int32_t) * g.NP;
+  d.plist = plist;
+  d.cnt = mem.arr<int32_t>((size_t)W * C);
+  if (pb.optimize) {
+    d.fld0 = mem.arr<float>((size_t)W * C);
+    d.fld2 = mem.arr<float>((size_t)W * C);
+    d.fld1 = (ncopies == 4) ? mem.arr<float>((size_t)W * C) : nullptr;
+  }
+  d.U0 = mem.arr<float>((size_t)W * g.NC * g.M * g.NP);
+  d.V0 = mem.arr<float>((size_t)W * g.NC * g.nwin * g.NP);
+  d.sv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
+  d.hv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
+  PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * (size_t)W * 4 * g.NC * g.NP, s));
+  d.acc = mem.arr<unsigned long long>((size_t)W * pb.K * C);
+  PGSVT_CK(cudaMemsetAsync(d.acc, 0, sizeof(unsigned long long) * (size_t)W * pb.K * C, s));
+  d.nblk_eval = eval_blocks(g);
+  d.nblk_mse = mse_blocks(g);
+  d.part_lin = mem.arr<double>((size_t)W * pb.K * d.nblk_eval);
+  d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
+  d.wc = mem.arr<WinConst>(W);
+  d.st = mem.arr<SearchState>(W);
+  d.counters = mem.arr<unsigned long long>(4);
+  PGSVT_CK(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned long long), s));
+  d.Y = Y_dev;
+  d.est = est_dev;
+  d.ncopies = ncopies;
+  d.nchains = 2 * g.fw;
+  const double vP = probe_vp();
+  d.d2neg = -1 * std::sqrt((1 - vP) / vP);
+  d.d2pos = std::sqrt(vP / (1 - vP));
+
+  // ARPS chains of every window, uploaded once
+  std::vector<ArpsChain> hch((size_t)nimg * d.nchains);
+  for (int t = 0; t < nimg; ++t) {
+    auto c = chains_for(t, g.fw, nimg, g.nwin);
+    std::copy(c.begin(), c.end(), hch.begin() + (size_t)t * d.nchains);
+  }
+  ArpsChain* dch = mem.arr<ArpsChain>(hch.size());
+  PGSVT_CK(cudaMemcpyAsync(dch, hch.data(), sizeof(ArpsChain) * hch.size(), cudaMemcpyHostToDevice, s));
+  stats.h2d += sizeof(ArpsChain) * hch.size();
+
+  // probes: one set for every window when seeded, else one per window
+  std::vector<int8_t> hp1, hp2;
+  int8_t* pd1 = nullptr;
+  int8_t* pd2 = nullptr;
+  if (pb.optimize) {
+    const bool shared = p.random_seed >= 0;
+    d.probe_stride = shared ? 0 : C;
+    const size_t nsets = shared ? 1 : (size_t)W;
+    pd1 = mem.arr<int8_t>(nsets * C);
+    pd2 = mem.arr<int8_t>(nsets * C);
+    hp1.resize(nsets * C);
+    hp2.resize(nsets * C);
+    if (shared) {
+      make_probes(p.random_seed, C, hp1.data(), hp2.data());
+      PGSVT_CK(cudaMemcpyAsync(pd1, hp1.data(), C, cudaMemcpyHostToDevice, s));
+      PGSVT_CK(cudaMemcpyAsync(pd2, hp2.data(), C, cudaMemcpyHostToDevice, s));
+      stats.h2d += 2 * C;
+    }
+    d.d1 = pd1;
+    d.d2code = pd2;
+  }
+
+  for (int win0 = 0; win0 < nimg; win0 += W) {
+    pb.W = std::min(W, nimg - win0);
+    d.win0 = win0;
+    d.chains = dch + (size_t)win0 * d.nchains;
+    if (pb.optimize && p.random_seed < 0) {  // fresh entropy per window (pgure.hpp:54-55)
+      PGSVT_CK(cudaStreamSynchronize(s));     // host buffers are reused
+      for (int w = 0; w < pb.W; ++w)
+        make_probes(-1, C, hp1.data() + (size_t)w * C, hp2.data() + (size_t)w * C);
+      PGSVT_CK(cudaMemcpyAsync(pd1, hp1.data(), (size_t)pb.W * C, cudaMemcpyHostToDevice, s));
+      PGSVT_CK(cudaMemcpyAsync(pd2, hp2.data(), (size_t)pb.W * C, cudaMemcpyHostToDevice, s));
+      stats.h2d += 2 * (size_t)pb.W * C;
+    }
+    check_launch(launch_window_setup(pb, d, s), stats, 2);
+    check_launch(launch_arps(pb, d, s), stats, pb.motion ? 2 : 1);
+    check_launch(launch_fields(pb, d, s), stats, 4);
+    check_launch(launch_svd(pb, d, s), stats);
+    check_launch(launch_search_init(pb, d, s), stats);
+    if (pb.optimize)
+      for (int r = 0; r < su.max_rounds; ++r) check_launch(launch_eval_round(pb, d, 0, s), stats, 3);
+    check_launch(launch_eval_round(pb, d, 1, s), stats);
+    check_launch(launch_output(pb, d, s), stats);
+  }
+  unsigned long long cnt[4];
+  PGSVT_CK(cudaMemcpyAsync(cnt, d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  PGSVT_CK(cudaStreamSynchronize(s));
+  stats.d2h += sizeof(cnt);
+  stats.evals += cnt[3];
+  if (p.verbose)
+    std::fprintf(stderr, "pgsvt: %dx%dx%d, bs=%d, nwin=%d, patches=%d, batch=%d, "
+                         "arps fp64 steps=%llu, svd warp-sweeps=%llu, fp64 tests=%llu\n",
+                 S, S, nimg, g.bs, g.nwin, g.NP, W, cnt[0], cnt[1], cnt[2]);
+}
+
+template <typename Fn>
+int guarded(pgsvt_status* st, Fn&& fn) {
+  const auto t0 = std::chrono::steady_clock::now();
+  Stats stats;
+  int code = PGSVT_OK, cuda = 0;
+  g_err.clear();
+  try {
+    fn(stats);
+  } catch (const Fail& f) {
+    code = f.code;
+    cuda = f.cuda;
+    g_err = f.what();
+  } catch (const std::exception& e) {
+    code = PGSVT_ERR_CUDA;
+    g_err = e.what();
+  }
+  if (st) {
+    st->code = code;
+    st->cuda_error = cuda;
+    st->kernel_launches = stats.launches;
+    st->h2d_bytes = stats.h2d;
+    st->d2h_bytes = stats.d2h;
+    st->risk_evals = stats.evals;
+    st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::snprintf(st->message, sizeof(st->message), "%s", g_err.c_str());
+  }
+  return code;
+}
+
+size_t dtype_size(int dtype) {
+  switch (dtype) {
+    case PGSVT_U8: return 1;
+    case PGSVT_U16: return 2;
+    case PGSVT_F32: return 4;
+    case PGSVT_F64: return 8;
+    default: throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid dtype");
+  }
+}
+
+void need_device() {
+  int n = 0;
+  const cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    throw Fail(PGSVT_ERR_CUDA, "no CUDA device available (this library has no CPU path)", (int)e);
+}
+
+// ---------------------------------------------------------------------------
+// Single-window pipeline for the component entry points: the window itself is
+// uploaded as an FP64 "sequence" of nwin slices, and the window constants come
+// from the host.
+
+struct OneWindow {
+  DevMem mem;
+  Problem pb;
+  DeviceBuffers d{};
+  Setup su;
+  cudaStream_t s = nullptr;
+  Stats stats;
+
+  OneWindow(const double* u, uint32_t S, uint32_t nwin, const pgsvt_params& p, int ref,
+            int out_slice) {
+    need_device();
+    if (nwin % 2 == 0 || nwin < 1) throw Fail(PGSVT_ERR_INVALID_ARG, "nwin must be odd");
+    if (S < p.block_size || p.block_size < 2 || p.block_size > 8)
+      throw Fail(PGSVT_ERR_INVALID_ARG, "bad block size");
+    if (!svd_supported((int)p.block_size, (int)nwin))
+      throw Fail(PGSVT_ERR_UNSUPPORTED, "window above 21 frames");
+    pgsvt_params q = p;
+    q.traj_length = nwin;  // the caller gives the window directly
+    if (p.block_size * p.block_size <= nwin) throw Fail(PGSVT_ERR_INVALID_ARG, "window too long for bs");
+    su = make_setup(q, (int)S, (int)nwin);
+    pb = make_problem(q, su);
+    pb.W = 1;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    const Geometry& g = pb.g;
+    const size_t C = g.cube();
+    double* x64 = mem.arr<double>(C);
+    float* xs = mem.arr<float>(C);
+    PGSVT_CK(cudaMemcpyAsync(x64, u, C * sizeof(double), cudaMemcpyHostToDevice, s));
+    check_launch(launch_convert(x64, PGSVT_F64, C, xs, nullptr, s), stats);
+    d.xs = xs;
+    d.x64 = x64;
+    double umax = u[0];
+    for (size_t i = 1; i < C; ++i) umax = std::max(umax, u[i]);
+    WinConst wc{};
+    wc.umax = umax;
+    wc.unorm = umax > 0 ? umax : 1.0;
+    wc.t = 0;
+    wc.s0 = 0;
+    wc.ref = ref;
+    wc.out_slice = out_slice;
+    wc.alpha = p.alpha;
+    if (p.compat_flags & PGSVT_COMPAT_SWAP_MU_SIGMA) {
+      wc.mu = p.sigma;
+      wc.sigma = p.mu;
+    } else {
+      wc.mu = p.mu;
+      wc.sigma = p.sigma;
+    }
+    wc.eps1 = (umax > 0 ? umax / umax : 1.0) * 0.0001;
+    wc.eps2 = 100 * wc.eps1;
+    d.wc = mem.arr<WinConst>(1);
+    PGSVT_CK(cudaMemcpyAsync(d.wc, &wc, sizeof(wc), cudaMemcpyHostToDevice, s));
+    d.u = mem.arr<float>(C);
+    d.pos = mem.arr<uint32_t>((size_t)g.nwin * g.P);
+    int32_t* plist = mem.arr<int32_t>(g.NP);
+    PGSVT_CK(cudaMemcpyAsync(plist, su.plist.data(), sizeof(int32_t) * g.NP, cudaMemcpyHostToDevice, s));
+    d.plist = plist;
+    d.cnt = mem.arr<int32_t>(C);
+    d.counters = mem.arr<unsigned long long>(4);
+    PGSVT_CK(cudaMemsetAsync(d.counters, 0, 32, s));
+    d.nchains = 2 * g.fw;
+    const double vP = probe_vp();
+    d.d2neg = -1 * std::sqrt((1 - vP) / vP);
+    d.d2pos = std::sqrt(vP / (1 - vP));
+    d.nblk_eval = eval_blocks(g);
+    d.nblk_mse = mse_blocks(g);
+    check_launch(launch_window_norm_only(pb, d, s), stats);
+  }
+  ~OneWindow() {
+    if (s) cudaStreamDestroy(s);
+  }
+
+  void set_positions(const int32_t* rows, const int32_t* cols) {
+    const Geometry& g = pb.g;
+    std::vector<uint32_t> h((size_t)g.nwin * g.P);
+    for (size_t i = 0; i < h.size(); ++i) {
+      if (rows[i] < 0 || cols[i] < 0 || rows[i] + g.bs > g.S || cols[i] + g.bs > g.S)
+        throw Fail(PGSVT_ERR_INVALID_ARG, "trajectory position outside the frame");
+      h[i] = (uint32_t)rows[i] | ((uint32_t)cols[i] << 16);
+    }
+    PGSVT_CK(cudaMemcpyAsync(d.pos, h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+  }
+
+  void alloc_factors(int ncopies) {
+    const Geometry& g = pb.g;
+    d.ncopies = ncopies;
+    d.U0 = mem.arr<float>((size_t)g.NC * g.M * g.NP);
+    d.V0 = mem.arr<float>((size_t)g.NC * g.nwin * g.NP);
+    d.sv = mem.arr<float>((size_t)4 * g.NC * g.NP);
+    d.hv = mem.arr<float>((size_t)4 * g.NC * g.NP);
+    PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * 4 * g.NC * g.NP, s));
+    d.acc = mem.arr<unsigned long long>((size_t)pb.K * g.cube());
+    PGSVT_CK(cudaMemsetAsync(d.acc, 0, sizeof(unsigned long long) * pb.K * g.cube(), s));
+    d.part_lin = mem.arr<double>((size_t)pb.K * d.nblk_eval);
+    d.part_mse = mem.arr<double>(std::max<size_t>((size_t)pb.K * d.nblk_mse, 256));
+    d.st = mem.arr<SearchState>(1);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int pgsvt_default_params(pgsvt_params* p) {
+  if (!p) return PGSVT_ERR_INVALID_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->traj_length = 15;
+  p->block_size = 4;
+  p->block_overlap = 1;
+  p->motion_window = 7;
+  p->median_size = 5;
+  p->noise_method = 4;
+  p->max_iter = 500;
+  p->n_jobs = -1;
+  p->random_seed = -1;
+  p->optimize_pgure = 1;
+  p->exp_weighting = 1;
+  p->motion_estimation = 1;
+  p->verbose = 0;
+  p->lambda = -1.0;
+  p->alpha = -1.0;
+  p->mu = -1.0;
+  p->sigma = -1.0;
+  p->tol = 1e-7;
+  p->compat_flags = PGSVT_COMPAT_ALL;
+  p->search_points = 8;
+  p->search_rounds = 4;
+  p->window_batch = 0;
+  p->lambda_hint = -1.0;
+  p->hint_span = 2.0;
+  return PGSVT_OK;
+}
+
+int pgsvt_denoise_device(const void* X_dev, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                         uint32_t nframes, double* Y_dev, double* est_dev, const pgsvt_params* p,
+                         void* stream, pgsvt_status* st) {
+  return guarded(st, [&](Stats& stats) {
+    if (!X_dev || !Y_dev || !est_dev || !p) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    need_device();
+    dtype_size(dtype);
+    validate(*p, nrows, ncols, nframes);
+    cudaStream_t s = (cudaStream_t)stream;
+    run_sequence(X_dev, dtype, (int)nrows, (int)nframes, Y_dev, est_dev, *p, s, stats);
+  });
+}
+
+int pgsvt_denoise(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols, uint32_t nframes,
+                  double* Y, double* estimates, const pgsvt_params* p, pgsvt_status* st) {
+  return guarded(st, [&](Stats& stats) {
+    if (!X || !Y || !estimates || !p) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    need_device();
+    const size_t es = dtype_size(dtype);
+    validate(*p, nrows, ncols, nframes);
+    const size_t n = (size_t)nrows * ncols * nframes;
+    DevMem mem;
+    cudaStream_t s;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    void* Xd = mem.get(n * es);
+    double* Yd = mem.arr<double>(n);
+    double* Ed = mem.arr<double>((size_t)nframes * 4);
+    PGSVT_CK(cudaMemcpyAsync(Xd, X, n * es, cudaMemcpyHostToDevice, s));
+    stats.h2d += n * es;
+    run_sequence(Xd, dtype, (int)nrows, (int)nframes, Yd, Ed, *p, s, stats);
+    PGSVT_CK(cudaMemcpyAsync(Y, Yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaMemcpyAsync(estimates, Ed, (size_t)nframes * 4 * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    stats.d2h += n * sizeof(double) + (size_t)nframes * 4 * sizeof(double);
+  });
+}
+
+int pgsvt_arps_window(const double* w, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                      uint32_t motion_window, uint32_t time_iter, uint32_t frame_window,
+                      uint32_t nimages, int32_t motion_estimation, uint32_t compat_flags,
+                      int32_t* rows, int32_t* cols) {
+  return guarded(nullptr, [&](Stats&) {
+    if (!w || !rows || !cols) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (nwin != 2 * frame_window + 1) throw Fail(PGSVT_ERR_INVALID_ARG, "nwin must be 2*frame_window+1");
+    if (nimages < nwin || time_iter >= nimages) throw Fail(PGSVT_ERR_INVALID_ARG, "bad time index");
+    if (motion_estimation && (motion_window < 2 || motion_window > (uint32_t)kMaxMW))
+      throw Fail(PGSVT_ERR_INVALID_ARG, "motion_window must be in [2, 15]");
+    pgsvt_params p;
+    pgsvt_default_params(&p);
+    p.block_size = block_size;
+    p.motion_window = motion_window;
+    p.motion_estimation = motion_estimation;
+    p.compat_flags = compat_flags;
+    const int t = (int)time_iter, tw = (int)frame_window, ni = (int)nimages;
+    int ref;
+    if (t < tw) ref = t;
+    else if (t >= ni - tw) ref = t - (ni - (int)nwin);
+    else ref = tw;
+    OneWindow ow(w, nrows, nwin, p, ref, ref);
+    const Geometry& g = ow.pb.g;
+    auto ch = chains_for(t, tw, ni, (int)nwin);
+    ArpsChain* dch = ow.mem.arr<ArpsChain>(ch.size());
+    PGSVT_CK(cudaMemcpyAsync(dch, ch.data(), sizeof(ArpsChain) * ch.size(), cudaMemcpyHostToDevice, ow.s));
+    ow.d.chains = dch;
+    PGSVT_CK(launch_arps(ow.pb, ow.d, ow.s));
+    std::vector<uint32_t> h((size_t)g.nwin * g.P);
+    PGSVT_CK(cudaMemcpyAsync(h.data(), ow.d.pos, h.size() * 4, cudaMemcpyDeviceToHost, ow.s));
+    PGSVT_CK(cudaStreamSynchronize(ow.s));
+    for (size_t i = 0; i < h.size(); ++i) {
+      rows[i] = (int32_t)(h[i] & 0xffffu);
+      cols[i] = (int32_t)(h[i] >> 16);
+    }
+  });
+}
+
+int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                     uint32_t block_overlap, const int32_t* rows, const int32_t* cols, float* S,
+                     uint32_t* npatch) {
+  return guarded(nullptr, [&](Stats&) {
+    if (!u || !rows || !cols || !npatch) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    pgsvt_params p;
+    pgsvt_default_params(&p);
+    p.block_size = block_size;
+    p.block_overlap = block_overlap;
+    p.optimize_pgure = 0;
+    p.lambda = 0.0;
+    OneWindow ow(u, nrows, nwin, p, (int)nwin / 2, (int)nwin / 2);
+    const Geometry& g = ow.pb.g;
+    ow.set_positions(rows, cols);
+    ow.alloc_factors(1);
+    PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
+    *npatch = (uint32_t)g.NP;
+    if (S) {
+      std::vector<float> h((size_t)g.NC * g.NP);
+      PGSVT_CK(cudaMemcpyAsync(h.data(), ow.d.sv, h.size() * 4, cudaMemcpyDeviceToHost, ow.s));
+      PGSVT_CK(cudaStreamSynchronize(ow.s));
+      for (int pi = 0; pi < g.NP; ++pi)
+        for (int i = 0; i < g.nwin; ++i) S[(size_t)pi * g.nwin + i] = h[(size_t)i * g.NP + pi];
+    }
+  });
+}
+
+int pgsvt_reconstruct_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                             uint32_t block_overlap, int32_t exp_weighting, const int32_t* rows,
+                             const int32_t* cols, double lambda, double* v) {
+  return guarded(nullptr, [&](Stats&) {
+    if (!u || !rows || !cols || !v) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (!(lambda >= 0)) throw Fail(PGSVT_ERR_INVALID_ARG, "lambda must be >= 0");
+    pgsvt_params p;
+    pgsvt_default_params(&p);
+    p.block_size = block_size;
+    p.block_overlap = block_overlap;
+    p.exp_weighting = exp_weighting;
+    p.optimize_pgure = 0;
+    p.lambda = lambda;
+    OneWindow ow(u, nrows, nwin, p, (int)nwin / 2, (int)nwin / 2);
+    const Geometry& g = ow.pb.g;
+    ow.set_positions(rows, cols);
+    ow.alloc_factors(1);
+    PGSVT_CK(cudaMemsetAsync(ow.d.cnt, 0, sizeof(int32_t) * g.cube(), ow.s));
+    PGSVT_CK(launch_fields(ow.pb, ow.d, ow.s));
+    PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
+    PGSVT_CK(launch_search_init(ow.pb, ow.d, ow.s));
+    PGSVT_CK(launch_eval_round(ow.pb, ow.d, 2, ow.s));
+    double* vd = ow.mem.arr<double>(g.cube());
+    PGSVT_CK(launch_cube_out(ow.pb, ow.d, vd, ow.s));
+    PGSVT_CK(cudaMemcpyAsync(v, vd, sizeof(double) * g.cube(), cudaMemcpyDeviceToHost, ow.s));
+    PGSVT_CK(cudaStreamSynchronize(ow.s));
+  });
+}
+
+int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                      uint32_t block_overlap, int32_t exp_weighting, const int32_t* rows,
+                      const int32_t* cols, double alpha, double mu, double sigma,
+                      int64_t random_seed, uint32_t compat_flags, const double* lambdas,
+                      uint32_t nl, double* risk) {
+  return guarded(nullptr, [&](Stats&) {
+    if (!u || !rows || !cols || !lambdas || !risk) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (alpha < 0 || mu < 0 || sigma < 0) throw Fail(PGSVT_ERR_INVALID_ARG, "noise parameters must be >= 0");
+    pgsvt_params p;
+    pgsvt_default_params(&p);
+    p.block_size = block_size;
+    p.block_overlap = block_overlap;
+    p.exp_weighting = exp_weighting;
+    p.optimize_pgure = 1;
+    p.alpha = alpha;
+    p.mu = mu;
+    p.sigma = sigma;
+    p.compat_flags = compat_flags;
+    p.random_seed = random_seed;
+    p.search_points = kMaxK;
+    OneWindow ow(u, nrows, nwin, p, (int)nwin / 2, (int)nwin / 2);
+    const Geometry& g = ow.pb.g;
+    const size_t C = g.cube();
+    ow.set_positions(rows, cols);
+    const int ncopies = (compat_flags & PGSVT_COMPAT_INT_DELTA1) ? 3 : 4;
+    ow.alloc_factors(ncopies);
+    ow.d.fld0 = ow.mem.arr<float>(C);
+    ow.d.fld2 = ow.mem.arr<float>(C);
+    ow.d.fld1 = ncopies == 4 ? ow.mem.arr<float>(C) : nullptr;
+    std::vector<int8_t> h1(C), h2(C);
+    make_probes(random_seed, C, h1.data(), h2.data());
+    int8_t* d1 = ow.mem.arr<int8_t>(C);
+    int8_t* d2 = ow.mem.arr<int8_t>(C);
+    PGSVT_CK(cudaMemcpyAsync(d1, h1.data(), C, cudaMemcpyHostToDevice, ow.s));
+    PGSVT_CK(cudaMemcpyAsync(d2, h2.data(), C, cudaMemcpyHostToDevice, ow.s));
+    ow.d.d1 = d1;
+    ow.d.d2code = d2;
+    ow.d.probe_stride = 0;
+    PGSVT_CK(launch_fields(ow.pb, ow.d, ow.s));
+    PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
+    double* out = ow.mem.arr<double>(kMaxK);
+    for (uint32_t j0 = 0; j0 < nl; j0 += kMaxK) {
+      const int n = (int)std::min<uint32_t>(kMaxK, nl - j0);
+      SearchState hs;
+      std::memset(&hs, 0, sizeof(hs));
+      for (int j = 0; j < n; ++j) hs.next[j] = lambdas[j0 + j];
+      hs.nnext = n;
+      hs.done = 0;
+      PGSVT_CK(cudaMemcpyAsync(ow.d.st, &hs, sizeof(hs), cudaMemcpyHostToDevice, ow.s));
+      PGSVT_CK(launch_risk_round(ow.pb, ow.d, out, ow.s));
+      PGSVT_CK(cudaMemcpyAsync(risk + j0, out, sizeof(double) * n, cudaMemcpyDeviceToHost, ow.s));
+      PGSVT_CK(cudaStreamSynchronize(ow.s));
+    }
+  });
+}
+
+const char* pgsvt_last_error(void) { return g_err.c_str(); }
+
+const char* pgsvt_version(void) { return "pgsvt-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

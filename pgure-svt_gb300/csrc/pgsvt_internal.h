@@ -1,0 +1,164 @@
+// pgsvt_internal.h — device-side data layout and kernel launchers of libpgsvt.
+//
+// One "window" is the reference's per-output-frame work item
+// (pguresvt.hpp:90-167): nwin = 2*fw+1 frames of an S x S sequence,
+// normalised by their maximum.  Windows are processed in batches of W on one
+// device; every buffer below holds W windows back to back.
+//
+// Layout in HBM (all column-major like the reference's Armadillo cubes):
+//   xs      f32 [nimg][S*S]       the input sequence, converted once
+//   x64     f64 [nimg][S*S]       only for f64 input: exact values for the
+//                                 FP64 ARPS tie-break path
+//   u       f32 [W][nwin][S*S]    normalised windows (u = x / umax)
+//   pos     u32 [W][nwin][P]      trajectory table: row | col << 16, where
+//                                 P = (S-bs+1)^2 ARPS positions (arps.hpp:42)
+//   cnt     i32 [W][nwin][S*S]    patch coverage per voxel (svt.hpp:157-159)
+//   fld0,2  f32 [W][nwin][S*S]    lambda-independent risk fields (see eval.cu)
+//   U0      f32 [W][NC][M][NP]    left singular vectors of copy 0 (patch
+//                                 fastest), columns sorted by singular value
+//   V0      f32 [W][NC][N][NP]    right singular vectors of copy 0
+//   sv,hv   f32 [W][4][NC][NP]    singular values and risk projections of
+//                                 copies 0 (clean), 1 (+eps2*delta2),
+//                                 2 (-eps2*delta2), 3 (+eps1*delta1)
+//   acc     i64 [W][K][nwin][S*S] fixed-point (2^-32) scatter accumulators
+// NP is the number of kept patches (svt.hpp:61-94), M = bs*bs, N = nwin,
+// NC = N rounded up to the kernel's even column count.
+#ifndef PGSVT_INTERNAL_H
+#define PGSVT_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pgsvt {
+
+constexpr int kMaxK = 16;          // lambda values per evaluation round
+constexpr int kMaxPts = 160;       // evaluated points kept per window
+constexpr int kMaxMW = 15;         // motion window supported by ARPS
+constexpr double kFixScale = 4294967296.0;  // 2^32 fixed-point scale
+
+// Per-window constants, computed on the device.
+struct WinConst {
+  double umax;     // window maximum (pguresvt.hpp:116)
+  double unorm;    // divisor of the normalisation: umax, or 1 for an all-zero
+                   // window (the reference's 0/0 ends as a zero output frame)
+  double sum_u;    // accu(u)
+  double alpha, mu, sigma;  // PGURE members (after the argument binding)
+  double eps1, eps2;
+  double start, upper;      // lambda search start point / upper bound
+  int32_t t;                // output frame index
+  int32_t s0;               // first sequence frame of the window
+  int32_t out_slice;        // window slice copied to the output
+  int32_t ref;              // ARPS reference slice
+};
+
+// Search state of one window (device-resident, advanced by k_search_step).
+// Phases: 0 = plain search, 1 = hinted search, 2 = plain search after a
+// hint whose best point fell on the edge of its grid.
+struct SearchState {
+  double lam[kMaxPts];
+  double risk[kMaxPts];
+  double next[kMaxK];   // lambda values of the pending round
+  double hint_lambda, hint_risk;
+  double final_lambda, final_risk;
+  int32_t npts, nnext, done, best;
+  int32_t phase, K, max_eval, rounds, zero_lo, rd, evals_phase, evals_total, first;
+};
+
+// ARPS chain table: for each window, up to 2*fw chains of <=2 frame pairs
+// (pairs sharing a motion slot, arps.hpp:121-130), executed in order.
+struct ArpsChain {
+  int8_t npairs;
+  int8_t a1[2], a2[2];
+};
+
+struct Geometry {
+  int S;        // frame side
+  int bs;       // patch side
+  int M;        // bs*bs
+  int nwin;     // window length
+  int fw;       // frame window
+  int Ntc;      // clamped trajectory length (pguresvt.hpp:57)
+  int P;        // ARPS positions
+  int NP;       // kept patches
+  int NC;       // padded column count of the SVD kernel
+  int mw;       // motion window
+  int nimg;
+  __host__ __device__ size_t F() const { return (size_t)S * S; }
+  __host__ __device__ size_t cube() const { return F() * nwin; }
+};
+
+struct Problem {
+  Geometry g;
+  int W;                 // windows in this batch
+  int K;                 // lambda values per round
+  int optimize, expw, motion, compat;
+  double alpha_c, mu_c, sigma_c;  // caller-side noise parameters
+  double lambda_user;
+  double tol;
+  int max_evals, rounds;
+  double hint, hint_span;
+};
+
+struct DeviceBuffers {
+  const float* xs;
+  const double* x64;
+  const double* fmax;      // per input frame maximum
+  float* u;
+  uint32_t* pos;
+  const int32_t* plist;    // kept patch -> position index
+  int32_t* pidx;           // position -> kept patch index (-1 if not kept)
+  int32_t* cnt;
+  float* fld0;
+  float* fld1;             // first-order field (only without the int-delta1 quirk)
+  float* fld2;
+  const int8_t* d1;        // probes, nwin*S*S per set
+  const int8_t* d2code;    // 1 -> -sqrt(vQ/vP), 0 -> sqrt(vP/vQ)
+  size_t probe_stride;     // 0: one set for all windows (seed >= 0), else per window
+  double d2neg, d2pos;     // the two delta2 values (pgure.hpp:173-183)
+  float* U0;
+  float* V0;
+  float* sv;
+  float* hv;
+  unsigned long long* acc;
+  double* part_lin;        // [W][K][nblk_eval]
+  double* part_mse;        // [W][K][nblk_mse]
+  WinConst* wc;
+  SearchState* st;
+  const ArpsChain* chains; // [W][2*fw]
+  int nchains;
+  double* Y;               // output [nimg][S*S] (double)
+  double* est;             // output estimates (nimg x 4)
+  unsigned long long* counters;  // [0] ARPS FP64 steps, [1] SVD warp-sweeps,
+                                 // [2] FP64 convergence tests, [3] risk evaluations
+  int win0;                // first window (output frame) of this batch
+  int ncopies;             // SVD copies decomposed (1, 3 or 4)
+  int nblk_eval, nblk_mse;
+};
+
+// launchers (each returns cudaGetLastError())
+cudaError_t launch_convert(const void* X, int dtype, size_t n, float* xs, double* x64,
+                           cudaStream_t s);
+cudaError_t launch_frame_max(const float* xs, const double* x64, int nimg, size_t F,
+                             double* fmax, cudaStream_t s);
+cudaError_t launch_window_setup(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_window_norm_only(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_arps(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_fields(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_search_init(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_eval_round(const Problem& pb, const DeviceBuffers& d, int final_pass,
+                              cudaStream_t s);
+cudaError_t launch_output(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_cube_out(const Problem& pb, const DeviceBuffers& d, double* v,
+                            cudaStream_t s);
+cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double* out,
+                              cudaStream_t s);
+
+int eval_blocks(const Geometry& g);
+int mse_blocks(const Geometry& g);
+int svd_columns(int nwin);
+bool svd_supported(int bs, int nwin);
+
+}  // namespace pgsvt
+
+#endif

@@ -1,0 +1,68 @@
+// svd.cu — batched one-sided Jacobi SVD of the Casorati matrices.
+//
+// Reference: SVT::Decompose (svt.hpp:58-118) gathers, for every kept patch,
+// the m x n Casorati matrix B (column k = the bs x bs patch of slice k at its
+// trajectory position, column-major within the patch) and calls
+// arma::svd_econ.  PGURE decomposes up to three more copies of the window
+// (pgure.hpp:62-91): U +/- eps2*delta2 and, without the integer-delta1 quirk,
+// U + eps1*delta1.
+//
+// GB300 mapping: one patch is held in the registers of LANES lanes, each lane
+// owning RPL consecutive rows of all NC (even, >= n) columns; 32/LANES patches
+// share a warp.  A sweep applies the NC-1 rounds of the round-robin ordering,
+// each round NC/2 disjoint Hestenes rotations; the only cross-lane traffic is
+// the butterfly sum of the column inner products.  Column norms are updated in
+// closed form during a sweep and recomputed exactly at its start.  A pair is
+// rotated when |a_i.a_j| > tol*|a_i||a_j|; for near-degenerate pairs close to
+// the threshold the inner product is re-evaluated in FP64 (exact products of
+// the FP32 entries) so that FP32 rounding cannot decide convergence.
+//
+// The epilogue needs no V accumulation: with u_i = a_i/s_i, the right vectors
+// are v_i = B^T u_i / s_i from a fresh gather of B, and the risk projections
+// h_i = u_i^T G v_i use the lambda-independent fields G (eval.cu).  Singular
+// triplets are stored sorted by decreasing s.
+#include "pgsvt_internal.h"
+
+namespace pgsvt {
+namespace svdk {
+template <int RPL, int LANES, int NC>
+cudaError_t run_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+}
+
+int svd_columns(int nwin) {
+  if (nwin <= 10) return 10;
+  if (nwin <= 16) return 16;
+  if (nwin <= 22) return 22;
+  return 0;
+}
+
+bool svd_supported(int bs, int nwin) {
+  // bs <= 4 clamps the window to bs*bs-1 <= 15 frames
+  return bs >= 2 && bs <= 8 && svd_columns(nwin) > 0;
+}
+
+// Kernel shapes: rows per lane x lanes per patch covers bs*bs rows; the
+// instantiations live in svd_i*.cu so that they compile in parallel.
+cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+  using namespace svdk;
+  const int M = pb.g.M, NC = pb.g.NC;
+  if (M <= 16) {  // bs 2..4
+    if (NC == 10) return run_svd<4, 4, 10>(pb, d, s);
+    if (NC == 16) return run_svd<4, 4, 16>(pb, d, s);
+  } else if (M <= 32) {  // bs 5
+    if (NC == 10) return run_svd<4, 8, 10>(pb, d, s);
+    if (NC == 16) return run_svd<4, 8, 16>(pb, d, s);
+    if (NC == 22) return run_svd<4, 8, 22>(pb, d, s);
+  } else if (M <= 40) {  // bs 6
+    if (NC == 10) return run_svd<5, 8, 10>(pb, d, s);
+    if (NC == 16) return run_svd<5, 8, 16>(pb, d, s);
+    if (NC == 22) return run_svd<5, 8, 22>(pb, d, s);
+  } else {  // bs 7, 8
+    if (NC == 10) return run_svd<4, 16, 10>(pb, d, s);
+    if (NC == 16) return run_svd<4, 16, 16>(pb, d, s);
+    if (NC == 22) return run_svd<4, 16, 22>(pb, d, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace pgsvt

@@ -1,0 +1,4 @@
+// svd_i4.cu — instantiations of the Jacobi SVD kernel (svd_kernel.cuh).
+#include "svd_kernel.cuh"
+
+PGSVT_INSTANTIATE_SVD(4, 16, 22)

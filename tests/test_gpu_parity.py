@@ -1,0 +1,224 @@
+"""GPU parity tests: the CUDA library through its C ABI against the FP64 oracle
+(live, on the same inputs) and against the frozen oracle vectors.
+
+Tolerances: ARPS trajectories are integer decisions and must be identical.
+The SVD, rebuild and reconstruction run in FP32 against an FP64 oracle, so
+they are compared with FP32-level tolerances stated per test; the risk sums
+are FP64 on both sides.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+
+
+def _window(X, t, fw):
+    nt = X.shape[2]
+    s0 = 0 if t < fw else (nt - 2 * fw - 1 if t >= nt - fw else t - fw)
+    u = X[:, :, s0:s0 + 2 * fw + 1].astype(np.float64)
+    return u / u.max()
+
+
+def _psnr(ref, x):
+    return 10 * np.log10(ref.max() ** 2 / np.mean((ref - x) ** 2))
+
+
+# ---- ARPS: motion vectors identical to the FP64 reference decisions
+
+def test_arps_matches_frozen_oracle(capi, g):
+    X = g["X"]
+    for t in (0, 3, 8, 15):
+        u = _window(X, t, 7)
+        rows, cols = capi.arps_window(u, 4, 7, t, 7, X.shape[2])
+        np.testing.assert_array_equal(rows, g["rows_%d" % t])
+        np.testing.assert_array_equal(cols, g["cols_%d" % t])
+
+
+@pytest.mark.parametrize("bs,mw,T", [(4, 7, 15), (4, 3, 15), (8, 7, 15), (6, 5, 9)])
+def test_arps_matches_live_oracle(capi, pkg, oracle, bs, mw, T):
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=21, side=48, nt=24)
+    ntc, fw, nwin = oracle.window_geometry(T, bs)
+    for t in (0, fw - 1, fw + 3, 24 - fw, 23):
+        u = _window(noisy, t, fw)
+        r0, c0 = oracle.arps_window(u, bs, mw, t, fw, 24)
+        r1, c1 = capi.arps_window(u, bs, mw, t, fw, 24)
+        np.testing.assert_array_equal(r1, r0)
+        np.testing.assert_array_equal(c1, c0)
+
+
+def test_arps_motion_off(capi, oracle, g):
+    u = g["u_8"]
+    for compat in (capi.COMPAT_ALL, capi.COMPAT_ALL & ~capi.COMPAT_ZERO_MOTION):
+        r0, c0 = oracle.arps_window(u, 4, 7, 8, 7, 16, motion=False, compat=compat)
+        r1, c1 = capi.arps_window(u, 4, 7, 8, 7, 16, motion=False, compat=compat)
+        np.testing.assert_array_equal(r1, r0)
+        np.testing.assert_array_equal(c1, c0)
+
+
+# ---- SVD: FP32 one-sided Jacobi vs FP64 LAPACK
+
+def test_singular_values(capi, g):
+    S0 = np.sort(g["S_8"], axis=1)[:, ::-1]
+    S1 = capi.svd_window(g["u_8"], 4, 1, g["rows_8"], g["cols_8"]).astype(np.float64)
+    smax = S0[:, :1]
+    err = np.abs(S1 - S0)
+    # absolute error relative to the patch's largest singular value
+    assert (err / smax).max() < 2e-5, (err / smax).max()
+    rel = err / np.maximum(S0, 1e-30)
+    big = S0 > 1e-3 * smax
+    print("singular values: max rel err %.3g, mean rel err %.3g (s > 1e-3 smax)"
+          % (rel[big].max(), rel[big].mean()))
+    assert rel[big].max() < 1e-3 and rel[big].mean() < 1e-5
+
+
+@pytest.mark.parametrize("bs,T", [(8, 15), (6, 21), (5, 9)])
+def test_singular_values_other_shapes(capi, pkg, oracle, bs, T):
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=4, side=24, nt=T)
+    ntc, fw, nwin = oracle.window_geometry(T, bs)
+    u = _window(noisy, fw, fw)
+    rows, cols = oracle.arps_window(u, bs, 5, fw, fw, T)
+    S0 = oracle.svd_window(u, bs, 1, rows, cols)
+    S1 = capi.svd_window(u, bs, 1, rows, cols).astype(np.float64)
+    assert (np.abs(S1 - S0) / S0[:, :1]).max() < 3e-5
+
+
+# ---- reconstruction at fixed lambda
+
+def test_reconstruct_window(capi, g):
+    v1 = capi.reconstruct_window(g["u_8"], 4, 1, g["rows_8"], g["cols_8"], 1.0)
+    v0 = g["v_8_l1"]
+    assert np.abs(v1 - v0).max() < 2e-5
+    assert np.abs(v1 - v0).mean() < 1e-6
+
+
+@pytest.mark.parametrize("lam,expw", [(0.0, True), (1e12, True), (0.02, False), (5.0, True)])
+def test_reconstruct_window_extremes(capi, oracle, g, lam, expw):
+    u, rows, cols = g["u_8"], g["rows_8"], g["cols_8"]
+    v0 = oracle.reconstruct_window(u, 4, 1, rows, cols, lam, expw=expw)
+    v1 = capi.reconstruct_window(u, 4, 1, rows, cols, lam, expw=expw)
+    assert np.abs(v1 - v0).max() < 3e-5
+
+
+# ---- PGURE risk (FP64 accumulation of FP32 factor terms)
+
+@pytest.mark.parametrize("mode", ["compat", "fixed"])
+def test_risk(capi, g, mode):
+    lams = g["risk_lams"]
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    compat = capi.COMPAT_ALL if mode == "compat" else 0
+    r1 = capi.risk_window(g["u_8"], 4, 1, g["rows_8"], g["cols_8"], lams, a, m, s, 11, compat)
+    r0 = g["risk_8_" + mode]
+    scale = np.abs(r0).max()
+    print(mode, "risk oracle", r0, "gpu", r1)
+    assert np.abs(r1 - r0).max() < 1e-4 * scale + 1e-9
+
+
+# ---- whole sequence through pgsvt_denoise
+
+def test_denoise_fixed_lambda_matches_oracle(capi, g):
+    p = capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1)
+    Y, est, st = capi.denoise(g["X"], p)
+    Y0 = g["Y_fixed"]
+    assert np.abs(Y - Y0).max() < 2e-5 * np.abs(Y0).max()
+    assert abs(_psnr(Y0, Y)) > 80  # GPU output within FP32 noise of the oracle
+    assert np.all(est[:, 0] == 0.1)
+    assert st.kernel_launches > 0
+
+
+def test_denoise_pgure_matches_oracle(capi, oracle, g):
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    p = capi.default_params(median_size=-1, random_seed=11, alpha=a, mu=m, sigma=s,
+                            search_points=8, search_rounds=2)
+    Y, est, st = capi.denoise(g["X"], p)
+    Y0, est0 = g["Y_pgure"], g["est_pgure"]
+    np.testing.assert_array_equal(est[:, 1:], est0[:, 1:])
+    # lambda: same search schedule, FP32 vs FP64 risks; compare the risk the
+    # oracle assigns to both choices (risk gap) and the output PSNR
+    X = g["X"].astype(np.float64)
+    gaps = []
+    for t in (0, 8, 15):
+        u = _window(X, t, 7)
+        rows, cols = oracle.arps_window(u, 4, 7, t, 7, 16)
+        r = oracle.risk_window(u, 4, 1, rows, cols, [est[t, 0], est0[t, 0]], a, m, s, 11)
+        gaps.append((r[0] - r[1]) / abs(r[1]))
+    print("lambda gpu", est[:, 0], "oracle", est0[:, 0], "risk gaps", gaps)
+    assert max(gaps) < 0.01
+    clean_like = Y0
+    assert np.abs(Y - Y0).max() < 5e-3 * np.abs(Y0).max()
+    assert st.risk_evals > 0
+
+
+def test_denoise_is_deterministic(capi, g):
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    p = capi.default_params(median_size=-1, random_seed=3, alpha=a, mu=m, sigma=s)
+    Y1, e1, _ = capi.denoise(g["X"], p)
+    Y2, e2, _ = capi.denoise(g["X"], p)
+    np.testing.assert_array_equal(Y1, Y2)
+    np.testing.assert_array_equal(e1, e2)
+
+
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32", "float64"])
+def test_input_dtypes(capi, oracle, pkg, dtype):
+    noisy, _, _ = pkg.synth.workload("plain_64", seed=2, side=32, nt=16)
+    X = np.clip(noisy, 0, 255 if dtype == "uint8" else 6e4).astype(dtype)
+    kw = dict(median_size=-1, optimize_pgure=0, lambda_=0.3)
+    Y, _, _ = capi.denoise(X, capi.default_params(**kw))
+    Y0, _, _ = oracle.denoise(X, n_jobs=4, **kw)
+    assert np.abs(Y - Y0).max() < 3e-5 * np.abs(Y0).max()
+
+
+def test_window_batching_does_not_change_results(capi, g):
+    kw = dict(median_size=-1, optimize_pgure=0, lambda_=0.1)
+    Y1, _, _ = capi.denoise(g["X"], capi.default_params(window_batch=1, **kw))
+    Y5, _, _ = capi.denoise(g["X"], capi.default_params(window_batch=5, **kw))
+    np.testing.assert_array_equal(Y1, Y5)
+
+
+def test_svt_estimator_on_gpu(pkg, g):
+    s = pkg.SVT(motion_filter=None, noise_alpha=float(g["alpha"]), noise_mu=float(g["mu"]),
+                noise_sigma=float(g["sigma"]), random_seed=11)
+    s.denoise(np.ascontiguousarray(g["X"]))
+    assert s.Y_.shape == g["X"].shape
+    assert np.all(s.lambda1s_ > 0) and np.all(s.noise_alphas_ == float(g["alpha"]))
+
+
+def test_errors(capi, pkg):
+    X = np.ones((16, 16, 16), np.float32)
+    p = capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1)
+    with pytest.raises(pkg.PgsvtError) as e:
+        capi.denoise(np.ones((16, 12, 16), np.float32), p)
+    assert e.value.code == capi.ERR_INVALID_ARG
+    Xn = X.copy()
+    Xn[1, 2, 3] = -1
+    with pytest.raises(pkg.PgsvtError) as e:
+        capi.denoise(Xn, p)
+    assert e.value.code == capi.ERR_NONFINITE
+    Xn[1, 2, 3] = np.nan
+    with pytest.raises(pkg.PgsvtError) as e:
+        capi.denoise(Xn, p)
+    assert e.value.code == capi.ERR_NONFINITE
+    with pytest.raises(pkg.PgsvtError) as e:
+        capi.denoise(X, capi.default_params(optimize_pgure=0, lambda_=0.1))  # median 5
+    assert e.value.code == capi.ERR_UNSUPPORTED
+    with pytest.raises(pkg.PgsvtError) as e:
+        capi.denoise(X[:, :, :8], p)  # shorter than the trajectory
+    assert e.value.code == capi.ERR_INVALID_ARG
+    # the library stays usable after errors
+    Y, _, _ = capi.denoise(X, p)
+    assert np.isfinite(Y).all()
+
+
+def test_all_zero_sequence(capi):
+    # umax = 0: the reference divides 0/0 and zeroes non-finite voxels
+    X = np.zeros((16, 16, 16), np.float32)
+    Y, _, _ = capi.denoise(X, capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1))
+    assert np.all(Y == 0)
