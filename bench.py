@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark: PGURE-optimal denoising throughput (output frames per second).
+
+Workload (default): the 512x512x200 float32 lattice+blob sequence, 4x4
+patches, trajectory 15, ARPS on (neighbourhood 7), PGURE lambda optimisation
+on, Poisson-Gaussian noise alpha=0.5, mu=1, sigma=3, seeded probes.  One step
+is one denoise of the whole sequence (200 output windows).
+
+value: frames/s with the sequence already resident in HBM (pgsvt_denoise_device
+on torch's current stream, CUDA events around the timed steps).
+e2e:   frames/s through pgsvt_denoise with pinned host buffers (host->device
+copy of the input and device->host copy of the result inside every step).
+cpu_baseline: the FP64 oracle port on the host cores, timed on a bounded sample.
+
+Run with torchrun for N > 1: every rank denoises its own sequence (weak
+scaling, no collective on the data path); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "frames/s at PGURE-optimal lambda (512^2, 4x4, T=15)"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+SM_COUNT = 152
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--side", type=int, default=512)
+    ap.add_argument("--frames", type=int, default=200)
+    ap.add_argument("--patch", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--hint", type=float, default=-1.0, help="lambda proposal (learned form)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-stride", type=int, default=0, help="patch stride of the CPU sample")
+    return ap.parse_args()
+
+
+def params(capi, a, m, s, bs, hint):
+    return capi.default_params(traj_length=15, block_size=bs, block_overlap=1, motion_window=7,
+                               median_size=-1, random_seed=7, optimize_pgure=1, alpha=a, mu=m,
+                               sigma=s, lambda_hint=hint)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.samples = []
+        self.proc = None
+        self.device = device
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for smp in self.samples:
+            try:
+                sm.append(float(smp[0]))
+                smax.append(float(smp[1]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, smp[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(side, frames, seed):
+    pkg = entry.load_package()
+    noisy, clean, (a, m, s) = pkg.synth.workload("lattice_512", seed=seed, side=side, nt=frames)
+    return noisy, (a, m, s)
+
+
+def svd_flops(m, n):
+    """Golub-Van Loan thin-SVD operation count 14mn^2 + 8n^3 per matrix."""
+    return 14 * m * n * n + 8 * n ** 3
+
+
+def cpu_baseline(noisy, nm, bs, evals_per_window, stride, threads, nsample):
+    """Oracle port timed on the host cores: one window per thread, every
+    `stride`-th patch position, `evals_per_window` risk evaluations."""
+    O = entry.load_oracle()
+    a, m, s = nm
+    nimg = noisy.shape[2]
+    first = max(0, nimg // 2 - nsample // 2)
+    t0 = time.perf_counter()
+    sec = O.time_sample(noisy, first, nsample, threads, stride, evals_per_window,
+                        traj_length=15, block_size=bs, motion_window=7, median_size=-1,
+                        random_seed=7, optimize_pgure=1, alpha=a, mu=m, sigma=s)
+    wall = time.perf_counter() - t0
+    return {"value": threads / sec, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": "%d windows (frames %d-%d) on %d threads, every %d-th patch position, "
+                      "%d risk evaluations/window; per-window time = %d x patch-proportional "
+                      "work + per-voxel work (%.1f s wall)"
+                      % (nsample, first, first + nsample - 1, threads, stride, evals_per_window,
+                         stride, wall),
+            "seconds_per_window": sec}
+
+
+def choose_stride(side, bs):
+    # about 1-3 s of single-thread work per sampled window
+    P = (side - bs + 1) ** 2
+    return max(1, P // 4096)
+
+
+def run_reference(args, rank):
+    """Reference arm: the oracle port (the reference does not build here)."""
+    if rank != 0:
+        return
+    noisy, nm = make_workload(args.side, args.frames, args.seed)
+    threads = os.cpu_count() or 1
+    stride = args.cpu_stride or choose_stride(args.side, args.patch)
+    evals = 40
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(noisy, nm, args.patch, evals, stride, threads, threads)
+        if i >= args.warmup:
+            vals.append(r)
+    v = statistics.median([r["value"] for r in vals])
+    line = {"metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.frames / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded blob+lattice sequence, Poisson-Gaussian noise)",
+            "config": {"workload": "lattice_512: %dx%dx%d f32, patch %d, T=15, ARPS mw=7, PGURE on"
+                                   % (args.side, args.side, args.frames, args.patch)},
+            "impl": "reference",
+            "cpu_baseline": {k: vals[-1][k] for k in ("kind", "cores", "sample")} | {"value": v},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = entry.load_package()
+    capi = pkg._capi
+    capi.load()
+    noisy, (a, m, s) = make_workload(args.side, args.frames, args.seed + rank)
+    S, nimg = args.side, args.frames
+    n = S * S * nimg
+    p = params(capi, a, m, s, args.patch, args.hint)
+
+    # ---- device-resident timing
+    x = torch.from_numpy(np.ascontiguousarray(noisy.ravel(order="F"))).cuda()
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    est = torch.empty(nimg * 4, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return capi.denoise_device(x.data_ptr(), capi.PGSVT_F32, S, S, nimg, y.data_ptr(),
+                                   est.data_ptr(), p, stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = []
+    for _ in range(args.steps):
+        stats.append(step())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nimg / (ms / 1e3)
+
+    # ---- end to end through pgsvt_denoise with pinned host buffers
+    xh = torch.from_numpy(np.ascontiguousarray(noisy.ravel(order="F"))).pin_memory()
+    yh = torch.empty(n, dtype=torch.float64).pin_memory()
+    eh = torch.empty(nimg * 4, dtype=torch.float64).pin_memory()
+    import ctypes
+    L = capi.load()
+
+    def e2e_step():
+        stt = capi.Status()
+        rc = L.pgsvt_denoise(ctypes.c_void_p(xh.data_ptr()), capi.PGSVT_F32, S, S, nimg,
+                             ctypes.c_void_p(yh.data_ptr()), ctypes.c_void_p(eh.data_ptr()),
+                             ctypes.byref(p), ctypes.byref(stt))
+        if rc != 0:
+            raise capi.PgsvtError(rc, stt.message.decode())
+        return stt
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ste = e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * nimg / e2e_s, "unit": "frames/s",
+           "h2d_bytes_per_step": int(xh.numel() * 4), "d2h_bytes_per_step": int((n + nimg * 4) * 8)}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (from the library's stage clocks)
+    st = stats[-1]
+    stage = {nm_: st.stage_seconds[i] for i, nm_ in enumerate(capi.STAGES)}
+    M, N = args.patch ** 2, 15
+    svd_t = st.stage_seconds[4] / max(1, st.svd_launches)
+    svd_flop = svd_flops(M, N) * st.svd_matrices / max(1, st.svd_launches)
+    peaks = json.load(open(PEAKS_PATH)) if os.path.exists(PEAKS_PATH) else {}
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+    roof = {"kernel": "k_svd (batched one-sided Jacobi, FP32 CUDA cores)", "bound": "fp32",
+            "achieved": svd_flop / svd_t / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": svd_flop / svd_t / 1e12 / fp32_peak,
+            "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x 2 flop x %.0f MHz "
+                           "(sm_max_mhz of MEASURED_PEAKS.json); MEASURED_PEAKS has no "
+                           "non-tensor FP32 figure" % sm_mhz,
+            "algorithmic_flops_per_launch": svd_flop, "avg_launch_ms": svd_t * 1e3,
+            "traffic": None}
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        roof["traffic"] = json.load(open(prof)).get("k_svd")
+
+    evals_per_window = max(1, round(st.risk_evals / max(1, st.windows)))
+    line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blob+lattice sequence, Poisson-Gaussian noise); input "
+                    "%.0f MB > L2 per step" % (noisy.nbytes / 1e6),
+            "config": {"workload": "lattice_512: %dx%dx%d f32, patch %d (m=%d), T=15, ARPS mw=7, "
+                                   "PGURE on, alpha=%g mu=%g sigma=%g, median off"
+                                   % (S, S, nimg, args.patch, M, a, m, s),
+                       "lambda_search": "plain" if args.hint <= 0 else "hinted %g" % args.hint,
+                       "l2": "input larger than L2 (no flush needed)"},
+            "e2e": e2e, "roofline": roof, "clocks": clk,
+            "gpu_launches": int(sum(x.kernel_launches for x in stats)),
+            "stage_seconds_per_step": stage,
+            "risk_evals_per_window": evals_per_window,
+            "arps_exact_steps": int(st.arps_exact_steps),
+            "svd_fp64_tests": int(st.svd_fp64_tests),
+            "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8)}
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        line["cpu_baseline"] = cpu_baseline(noisy, (a, m, s), args.patch, evals_per_window,
+                                            args.cpu_stride or choose_stride(S, args.patch),
+                                            threads, threads)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -98,6 +98,8 @@ typedef struct {
   uint32_t window_batch;    /* windows in flight on the device (0: auto)*/
   double lambda_hint;       /* >0: narrow search around this proposal   */
   double hint_span;         /* bracket [hint/span, hint*span] (0: 2.0)  */
+  uint32_t frame_begin;     /* output frames [frame_begin, frame_end) are */
+  uint32_t frame_end;       /* computed (0,0: all); others are left zero  */
 } pgsvt_params;
 
 /* Per-call report.  All times are wall seconds measured by the library. */
@@ -110,6 +112,16 @@ typedef struct {
   uint64_t h2d_bytes;       /* host->device bytes copied                  */
   uint64_t d2h_bytes;       /* device->host bytes copied                  */
   double seconds;           /* whole call                                 */
+  /* device time per stage (CUDA events on the call's stream):
+   * [0] convert + frame maxima  [1] window normalisation  [2] ARPS
+   * [3] coverage + risk fields  [4] SVD  [5] lambda search rounds
+   * [6] final reconstruction + output  [7] uploads between batches       */
+  double stage_seconds[8];
+  uint64_t svd_launches;    /* launches of the SVD kernel                 */
+  uint64_t svd_matrices;    /* Casorati matrices decomposed               */
+  uint64_t arps_exact_steps;/* ARPS diamond steps decided in FP64         */
+  uint64_t svd_fp64_tests;  /* Jacobi convergence tests decided in FP64   */
+  uint64_t svd_warp_sweeps; /* Jacobi sweeps summed over warps            */
   char message[256];        /* human-readable error / note                */
 } pgsvt_status;
 

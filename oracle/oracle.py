@@ -36,7 +36,8 @@ class OrcParams(ctypes.Structure):
         ("tol", ctypes.c_double), ("compat_flags", ctypes.c_uint32),
         ("search_points", ctypes.c_uint32), ("search_rounds", ctypes.c_uint32),
         ("window_batch", ctypes.c_uint32), ("lambda_hint", ctypes.c_double),
-        ("hint_span", ctypes.c_double),
+        ("hint_span", ctypes.c_double), ("frame_begin", ctypes.c_uint32),
+        ("frame_end", ctypes.c_uint32),
     ]
 
 
@@ -50,7 +51,8 @@ DEFAULTS = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7,
                 optimize_pgure=1, exp_weighting=1, motion_estimation=1, verbose=0,
                 lambda_=-1.0, alpha=-1.0, mu=-1.0, sigma=-1.0, tol=1e-7,
                 compat_flags=COMPAT_ALL, search_points=8, search_rounds=4,
-                window_batch=0, lambda_hint=-1.0, hint_span=2.0)
+                window_batch=0, lambda_hint=-1.0, hint_span=2.0, frame_begin=0,
+                frame_end=0)
 
 _lib = None
 

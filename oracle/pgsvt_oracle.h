@@ -32,6 +32,7 @@ typedef struct {
   double lambda, alpha, mu, sigma, tol;
   uint32_t compat_flags, search_points, search_rounds, window_batch;
   double lambda_hint, hint_span;
+  uint32_t frame_begin, frame_end;
 } orc_params;
 
 typedef struct {

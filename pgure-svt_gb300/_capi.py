@@ -44,8 +44,12 @@ class Params(ctypes.Structure):
         ("tol", ctypes.c_double), ("compat_flags", ctypes.c_uint32),
         ("search_points", ctypes.c_uint32), ("search_rounds", ctypes.c_uint32),
         ("window_batch", ctypes.c_uint32), ("lambda_hint", ctypes.c_double),
-        ("hint_span", ctypes.c_double),
+        ("hint_span", ctypes.c_double), ("frame_begin", ctypes.c_uint32),
+        ("frame_end", ctypes.c_uint32),
     ]
+
+
+STAGES = ("convert", "normalise", "arps", "fields", "svd", "search", "output", "uploads")
 
 
 class Status(ctypes.Structure):
@@ -54,6 +58,9 @@ class Status(ctypes.Structure):
         ("windows", ctypes.c_uint64), ("risk_evals", ctypes.c_uint64),
         ("kernel_launches", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
         ("d2h_bytes", ctypes.c_uint64), ("seconds", ctypes.c_double),
+        ("stage_seconds", ctypes.c_double * 8), ("svd_launches", ctypes.c_uint64),
+        ("svd_matrices", ctypes.c_uint64), ("arps_exact_steps", ctypes.c_uint64),
+        ("svd_fp64_tests", ctypes.c_uint64), ("svd_warp_sweeps", ctypes.c_uint64),
         ("message", ctypes.c_char * 256),
     ]
 

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -106,6 +107,26 @@ std::vector<int32_t> patch_list(int S, int bs, int ov) {
   return std::vector<int32_t>(v.begin(), v.end());
 }
 
+// Processing order of the kept patches: 8 x 4 tiles of grid positions (rows
+// fastest), so the 32 patches of a warp cover a compact region of every slice
+// and their rebuilt blocks overlap (k_eval).  The order has no effect on the
+// results: the overlap sums are integer sums.
+std::vector<int32_t> tile_order(const std::vector<int32_t>& plist, int S, int bs) {
+  const int n1 = S - bs + 1, ti = (n1 + 7) / 8;
+  std::vector<std::pair<int64_t, int32_t>> key;
+  key.reserve(plist.size());
+  for (int32_t it : plist) {
+    const int i = it % n1, j = it / n1;
+    const int64_t tk = ((int64_t)(j / 4) * ti + i / 8) * 32 + (j % 4) * 8 + (i % 8);
+    key.push_back({tk, it});
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> out;
+  out.reserve(key.size());
+  for (auto& kv : key) out.push_back(kv.second);
+  return out;
+}
+
 // Frame pairs of MotionEstimator::Estimate (arps.hpp:52-134) grouped into
 // chains of pairs that share a motion slot (the only data dependence).
 std::vector<ArpsChain> chains_for(int t, int tw, int nimg, int nwin) {
@@ -158,7 +179,37 @@ struct DevMem {
 };
 
 struct Stats {
-  uint64_t launches = 0, h2d = 0, d2h = 0, evals = 0;
+  uint64_t launches = 0, h2d = 0, d2h = 0, evals = 0, windows = 0;
+  uint64_t svd_launches = 0, svd_matrices = 0, arps_exact = 0, svd_fp64 = 0, svd_sweeps = 0;
+  double stage[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+// Device time per pipeline stage: an event is recorded on the stream at each
+// stage boundary and the intervals are summed once the stream is drained.
+class StageClock {
+ public:
+  explicit StageClock(cudaStream_t s) : s_(s) {}
+  ~StageClock() {
+    for (auto& m : marks_) cudaEventDestroy(m.ev);
+  }
+  void mark(int stage) {  // the interval from the previous mark belongs to `stage`
+    cudaEvent_t e;
+    PGSVT_CK(cudaEventCreate(&e));
+    PGSVT_CK(cudaEventRecord(e, s_));
+    marks_.push_back({e, stage});
+  }
+  void accumulate(double* out) const {
+    for (size_t i = 1; i < marks_.size(); ++i) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, marks_[i - 1].ev, marks_[i].ev) == cudaSuccess && ms > 0)
+        out[marks_[i].stage] += ms * 1e-3;
+    }
+  }
+
+ private:
+  struct Mark { cudaEvent_t ev; int stage; };
+  cudaStream_t s_;
+  std::vector<Mark> marks_;
 };
 
 void check_launch(cudaError_t e, Stats& s, int n = 1) {
@@ -201,7 +252,8 @@ void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
 struct Setup {
   Geometry g;
   int K, rounds, max_rounds;
-  std::vector<int32_t> plist;
+  std::vector<int32_t> sorted;  // kept patches in the reference's (sorted) order
+  std::vector<int32_t> plist;   // processing order
 };
 
 Setup make_setup(const pgsvt_params& p, int S, int nimg) {
@@ -214,7 +266,8 @@ Setup make_setup(const pgsvt_params& p, int S, int nimg) {
   g.fw = g.Ntc / 2;                                                   // pguresvt.hpp:58
   g.nwin = 2 * g.fw + 1;
   g.P = (S - g.bs + 1) * (S - g.bs + 1);
-  s.plist = patch_list(S, g.bs, (int)p.block_overlap);
+  s.sorted = patch_list(S, g.bs, (int)p.block_overlap);
+  s.plist = tile_order(s.sorted, S, g.bs);
   g.NP = (int)s.plist.size();
   g.NC = svd_columns(g.nwin);
   g.mw = (int)p.motion_window;
@@ -247,11 +300,12 @@ Problem make_problem(const pgsvt_params& p, const Setup& su) {
   pb.rounds = su.rounds;
   pb.hint = p.lambda_hint;
   pb.hint_span = p.hint_span > 1.0 ? p.hint_span : 2.0;
+  pb.acc64 = 0;
   return pb;
 }
 
 // Bytes of device memory one window of a batch needs.
-size_t window_bytes(const Problem& pb, int ncopies) {
+size_t window_bytes(const Problem& pb) {
   const Geometry& g = pb.g;
   const size_t C = g.cube(), NP = g.NP, NC = g.NC;
   size_t b = 0;
@@ -261,15 +315,27 @@ size_t window_bytes(const Problem& pb, int ncopies) {
   b += C * 4 * 3;                   // fields
   b += NC * g.M * NP * 4;           // U0
   b += NC * g.nwin * NP * 4;        // V0
-  b += 2 * 4 * NC * NP * 4;         // sv, hv
-  b += (size_t)pb.K * C * 8;        // acc
+  b += 2 * 4 * NC * NP * 4 + NP * 4;  // sv, hv, nlive0
+  b += (size_t)pb.K * C * (pb.acc64 ? 8 : 4);  // acc
   b += (size_t)pb.K * ((NP + 31) / 32 + mse_blocks(g)) * 8 + 256 * 8;  // partials
   b += sizeof(WinConst) + sizeof(SearchState) + 2 * (size_t)g.fw * sizeof(ArpsChain);
-  (void)ncopies;
   return b;
 }
 
+// Batch buffers and bookkeeping of one stream.
+struct Lane {
+  cudaStream_t s = nullptr;
+  bool own = false;
+  DeviceBuffers d{};
+  std::vector<int8_t> hp1, hp2;
+  int8_t* pd1 = nullptr;
+  int8_t* pd2 = nullptr;
+  std::unique_ptr<StageClock> clk;
+};
+
 // The per-sequence engine.  X_dev holds the input (dtype) on the device.
+// Windows are processed in batches of W; batches go round-robin to NS
+// streams, so one batch's lambda search overlaps another batch's SVD.
 void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, double* est_dev,
                   const pgsvt_params& p, cudaStream_t s, Stats& stats) {
   Setup su = make_setup(p, S, nimg);
@@ -281,8 +347,11 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   float* xs = mem.arr<float>((size_t)nimg * F);
   double* x64 = (dtype == PGSVT_F64) ? mem.arr<double>((size_t)nimg * F) : nullptr;
   double* fmx = mem.arr<double>(nimg);
+  StageClock clk0(s);
+  clk0.mark(0);
   check_launch(launch_convert(X_dev, dtype, (size_t)nimg * F, xs, x64, s), stats);
   check_launch(launch_frame_max(xs, x64, nimg, F, fmx, s), stats);
+  clk0.mark(0);
   std::vector<double> hmax(nimg);
   PGSVT_CK(cudaMemcpyAsync(hmax.data(), fmx, sizeof(double) * nimg, cudaMemcpyDeviceToHost, s));
   PGSVT_CK(cudaStreamSynchronize(s));
@@ -291,118 +360,195 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
 
   const int ncopies = !pb.optimize ? 1 : ((pb.compat & PGSVT_COMPAT_INT_DELTA1) ? 3 : 4);
-  // batch size
+  // zero-motion quirk: every patch lands on the (0,0) block of the other
+  // slices, beyond the int32 range
+  pb.acc64 = (!pb.motion && (pb.compat & PGSVT_COMPAT_ZERO_MOTION)) ? 1 : 0;
+  int fb = (int)p.frame_begin, fe = (int)p.frame_end;
+  if (fb == 0 && fe == 0) fe = nimg;
+  if (fb < 0 || fe > nimg || fb >= fe) throw Fail(PGSVT_ERR_INVALID_ARG, "bad frame range");
+  const int nwinds = fe - fb;
+  // batch size: about half a million kept patches per batch
+  int W = p.window_batch ? (int)p.window_batch
+                         : (int)std::max<int64_t>(1, (500000 + g.NP - 1) / (int64_t)g.NP);
+  W = std::max(1, std::min({W, nwinds, 32}));
+  const int nbatches = (nwinds + W - 1) / W;
+  int NS = std::min(3, nbatches);
   size_t freeb = 0, totb = 0;
   PGSVT_CK(cudaMemGetInfo(&freeb, &totb));
-  const size_t per = window_bytes(pb, ncopies);
-  const size_t budget = std::min<size_t>(freeb / 2, (size_t)48 << 30);
-  int W = p.window_batch ? (int)p.window_batch : (int)std::max<size_t>(1, budget / per);
-  W = std::max(1, std::min({W, nimg, 32}));
-  if ((size_t)W * per > freeb) throw Fail(PGSVT_ERR_OOM, "not enough device memory for one window");
+  const size_t per = window_bytes(pb);
+  while (NS > 1 && (size_t)NS * W * per > freeb / 2) --NS;
+  while (W > 1 && (size_t)NS * W * per > freeb / 2) --W;
+  if ((size_t)NS * W * per > freeb) throw Fail(PGSVT_ERR_OOM, "not enough device memory for one window");
 
-  // batch buffers
-  DeviceBuffers d{};
-  d.xs = xs;
-  d.x64 = x64;
-  d.fmax = fmx;
-  d.u = mem.arr<float>((size_t)W * C);
-  d.pos = mem.arr<uint32_t>((size_t)W * g.nwin * g.P);
+  // sequence-level tables shared by the streams
   int32_t* plist = mem.arr<int32_t>(g.NP);
   PGSVT_CK(cudaMemcpyAsync(plist, su.plist.data(), sizeof(int32_t) * g.NP, cudaMemcpyHostToDevice, s));
   stats.h2d += sizeof(int32_t) * g.NP;
-  d.plist = plist;
-  d.cnt = mem.arr<int32_t>((size_t)W * C);
-  if (pb.optimize) {
-    d.fld0 = mem.arr<float>((size_t)W * C);
-    d.fld2 = mem.arr<float>((size_t)W * C);
-    d.fld1 = (ncopies == 4) ? mem.arr<float>((size_t)W * C) : nullptr;
-  }
-  d.U0 = mem.arr<float>((size_t)W * g.NC * g.M * g.NP);
-  d.V0 = mem.arr<float>((size_t)W * g.NC * g.nwin * g.NP);
-  d.sv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
-  d.hv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
-  PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * (size_t)W * 4 * g.NC * g.NP, s));
-  d.acc = mem.arr<unsigned long long>((size_t)W * pb.K * C);
-  PGSVT_CK(cudaMemsetAsync(d.acc, 0, sizeof(unsigned long long) * (size_t)W * pb.K * C, s));
-  d.nblk_eval = eval_blocks(g);
-  d.nblk_mse = mse_blocks(g);
-  d.part_lin = mem.arr<double>((size_t)W * pb.K * d.nblk_eval);
-  d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
-  d.wc = mem.arr<WinConst>(W);
-  d.st = mem.arr<SearchState>(W);
-  d.counters = mem.arr<unsigned long long>(4);
-  PGSVT_CK(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned long long), s));
-  d.Y = Y_dev;
-  d.est = est_dev;
-  d.ncopies = ncopies;
-  d.nchains = 2 * g.fw;
-  const double vP = probe_vp();
-  d.d2neg = -1 * std::sqrt((1 - vP) / vP);
-  d.d2pos = std::sqrt(vP / (1 - vP));
-
-  // ARPS chains of every window, uploaded once
-  std::vector<ArpsChain> hch((size_t)nimg * d.nchains);
+  const int nchains = 2 * g.fw;
+  std::vector<ArpsChain> hch((size_t)nimg * nchains);
   for (int t = 0; t < nimg; ++t) {
     auto c = chains_for(t, g.fw, nimg, g.nwin);
-    std::copy(c.begin(), c.end(), hch.begin() + (size_t)t * d.nchains);
+    std::copy(c.begin(), c.end(), hch.begin() + (size_t)t * nchains);
   }
   ArpsChain* dch = mem.arr<ArpsChain>(hch.size());
   PGSVT_CK(cudaMemcpyAsync(dch, hch.data(), sizeof(ArpsChain) * hch.size(), cudaMemcpyHostToDevice, s));
   stats.h2d += sizeof(ArpsChain) * hch.size();
+  unsigned long long* counters = mem.arr<unsigned long long>(4);
+  PGSVT_CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+  const double vP = probe_vp();
+  const bool shared_probes = p.random_seed >= 0;
+  int8_t* sp1 = nullptr;
+  int8_t* sp2 = nullptr;
+  if (pb.optimize && shared_probes) {  // one probe set for every window (pgure.hpp:52-59)
+    std::vector<int8_t> h1(C), h2(C);
+    make_probes(p.random_seed, C, h1.data(), h2.data());
+    sp1 = mem.arr<int8_t>(C);
+    sp2 = mem.arr<int8_t>(C);
+    PGSVT_CK(cudaMemcpyAsync(sp1, h1.data(), C, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(sp2, h2.data(), C, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaStreamSynchronize(s));  // h1/h2 go out of scope
+    stats.h2d += 2 * C;
+  }
+  if (fb > 0 || fe < nimg) {
+    PGSVT_CK(cudaMemsetAsync(Y_dev, 0, sizeof(double) * (size_t)nimg * F, s));
+    PGSVT_CK(cudaMemsetAsync(est_dev, 0, sizeof(double) * (size_t)nimg * 4, s));
+  }
+  cudaEvent_t ready;
+  PGSVT_CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } evg{ready};
+  PGSVT_CK(cudaEventRecord(ready, s));
 
-  // probes: one set for every window when seeded, else one per window
-  std::vector<int8_t> hp1, hp2;
-  int8_t* pd1 = nullptr;
-  int8_t* pd2 = nullptr;
-  if (pb.optimize) {
-    const bool shared = p.random_seed >= 0;
-    d.probe_stride = shared ? 0 : C;
-    const size_t nsets = shared ? 1 : (size_t)W;
-    pd1 = mem.arr<int8_t>(nsets * C);
-    pd2 = mem.arr<int8_t>(nsets * C);
-    hp1.resize(nsets * C);
-    hp2.resize(nsets * C);
-    if (shared) {
-      make_probes(p.random_seed, C, hp1.data(), hp2.data());
-      PGSVT_CK(cudaMemcpyAsync(pd1, hp1.data(), C, cudaMemcpyHostToDevice, s));
-      PGSVT_CK(cudaMemcpyAsync(pd2, hp2.data(), C, cudaMemcpyHostToDevice, s));
-      stats.h2d += 2 * C;
+  std::vector<Lane> lanes(NS);
+  struct LaneGuard {
+    std::vector<Lane>& l;
+    ~LaneGuard() {
+      for (auto& x : l) {
+        x.clk.reset();
+        if (x.own && x.s) cudaStreamDestroy(x.s);
+      }
     }
-    d.d1 = pd1;
-    d.d2code = pd2;
+  } lg{lanes};
+  for (int li = 0; li < NS; ++li) {
+    Lane& L = lanes[li];
+    if (li == 0) {
+      L.s = s;
+    } else {
+      PGSVT_CK(cudaStreamCreateWithFlags(&L.s, cudaStreamNonBlocking));
+      L.own = true;
+      PGSVT_CK(cudaStreamWaitEvent(L.s, ready, 0));
+    }
+    L.clk.reset(new StageClock(L.s));
+    DeviceBuffers& d = L.d;
+    d.xs = xs;
+    d.x64 = x64;
+    d.fmax = fmx;
+    d.plist = plist;
+    d.counters = counters;
+    d.Y = Y_dev;
+    d.est = est_dev;
+    d.ncopies = ncopies;
+    d.nchains = nchains;
+    d.d2neg = -1 * std::sqrt((1 - vP) / vP);
+    d.d2pos = std::sqrt(vP / (1 - vP));
+    d.u = mem.arr<float>((size_t)W * C);
+    d.pos = mem.arr<uint32_t>((size_t)W * g.nwin * g.P);
+    d.cnt = mem.arr<int32_t>((size_t)W * C);
+    if (pb.optimize) {
+      d.fld0 = mem.arr<float>((size_t)W * C);
+      d.fld2 = mem.arr<float>((size_t)W * C);
+      d.fld1 = (ncopies == 4) ? mem.arr<float>((size_t)W * C) : nullptr;
+    }
+    d.U0 = mem.arr<float>((size_t)W * g.NC * g.M * g.NP);
+    d.V0 = mem.arr<float>((size_t)W * g.NC * g.nwin * g.NP);
+    d.sv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
+    d.hv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
+    d.nlive0 = mem.arr<int32_t>((size_t)W * g.NP);
+    PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * (size_t)W * 4 * g.NC * g.NP, L.s));
+    const size_t accb = (size_t)W * pb.K * C * (pb.acc64 ? 8 : 4);
+    d.acc = mem.get(accb);
+    PGSVT_CK(cudaMemsetAsync(d.acc, 0, accb, L.s));
+    d.nblk_eval = eval_blocks(g);
+    d.nblk_mse = mse_blocks(g);
+    d.part_lin = mem.arr<double>((size_t)W * pb.K * d.nblk_eval);
+    d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
+    d.wc = mem.arr<WinConst>(W);
+    d.st = mem.arr<SearchState>(W);
+    if (pb.optimize) {
+      if (shared_probes) {
+        d.d1 = sp1;
+        d.d2code = sp2;
+        d.probe_stride = 0;
+      } else {  // fresh entropy per window (pgure.hpp:54-55)
+        L.pd1 = mem.arr<int8_t>((size_t)W * C);
+        L.pd2 = mem.arr<int8_t>((size_t)W * C);
+        L.hp1.resize((size_t)W * C);
+        L.hp2.resize((size_t)W * C);
+        d.d1 = L.pd1;
+        d.d2code = L.pd2;
+        d.probe_stride = C;
+      }
+    }
   }
 
-  for (int win0 = 0; win0 < nimg; win0 += W) {
-    pb.W = std::min(W, nimg - win0);
+  int bi = 0;
+  for (int win0 = fb; win0 < fe; win0 += W, ++bi) {
+    Lane& L = lanes[bi % NS];
+    DeviceBuffers& d = L.d;
+    Problem pbb = pb;
+    pbb.W = std::min(W, fe - win0);
     d.win0 = win0;
-    d.chains = dch + (size_t)win0 * d.nchains;
-    if (pb.optimize && p.random_seed < 0) {  // fresh entropy per window (pgure.hpp:54-55)
-      PGSVT_CK(cudaStreamSynchronize(s));     // host buffers are reused
-      for (int w = 0; w < pb.W; ++w)
-        make_probes(-1, C, hp1.data() + (size_t)w * C, hp2.data() + (size_t)w * C);
-      PGSVT_CK(cudaMemcpyAsync(pd1, hp1.data(), (size_t)pb.W * C, cudaMemcpyHostToDevice, s));
-      PGSVT_CK(cudaMemcpyAsync(pd2, hp2.data(), (size_t)pb.W * C, cudaMemcpyHostToDevice, s));
-      stats.h2d += 2 * (size_t)pb.W * C;
+    d.chains = dch + (size_t)win0 * nchains;
+    StageClock& clk = *L.clk;
+    if (pb.optimize && !shared_probes) {
+      PGSVT_CK(cudaStreamSynchronize(L.s));  // the lane's host buffers are reused
+      for (int w = 0; w < pbb.W; ++w)
+        make_probes(-1, C, L.hp1.data() + (size_t)w * C, L.hp2.data() + (size_t)w * C);
+      PGSVT_CK(cudaMemcpyAsync(L.pd1, L.hp1.data(), (size_t)pbb.W * C, cudaMemcpyHostToDevice, L.s));
+      PGSVT_CK(cudaMemcpyAsync(L.pd2, L.hp2.data(), (size_t)pbb.W * C, cudaMemcpyHostToDevice, L.s));
+      stats.h2d += 2 * (size_t)pbb.W * C;
     }
-    check_launch(launch_window_setup(pb, d, s), stats, 2);
-    check_launch(launch_arps(pb, d, s), stats, pb.motion ? 2 : 1);
-    check_launch(launch_fields(pb, d, s), stats, 4);
-    check_launch(launch_svd(pb, d, s), stats);
-    check_launch(launch_search_init(pb, d, s), stats);
-    if (pb.optimize)
-      for (int r = 0; r < su.max_rounds; ++r) check_launch(launch_eval_round(pb, d, 0, s), stats, 3);
-    check_launch(launch_eval_round(pb, d, 1, s), stats);
-    check_launch(launch_output(pb, d, s), stats);
+    clk.mark(7);  // probe uploads and other gaps
+    check_launch(launch_window_setup(pbb, d, L.s), stats, 2);
+    clk.mark(1);
+    check_launch(launch_arps(pbb, d, L.s), stats, pbb.motion ? 2 : 1);
+    clk.mark(2);
+    check_launch(launch_fields(pbb, d, L.s), stats, 4);
+    check_launch(launch_search_init(pbb, d, L.s), stats);  // sets the lambda range
+    clk.mark(3);
+    check_launch(launch_svd(pbb, d, L.s), stats);
+    clk.mark(4);
+    stats.svd_launches += 1;
+    stats.svd_matrices += (uint64_t)pbb.W * ncopies * g.NP;
+    stats.windows += pbb.W;
+    if (pbb.optimize)
+      for (int r = 0; r < su.max_rounds; ++r) check_launch(launch_eval_round(pbb, d, 0, L.s), stats, 3);
+    clk.mark(5);
+    check_launch(launch_eval_round(pbb, d, 1, L.s), stats);
+    check_launch(launch_output(pbb, d, L.s), stats);
+    clk.mark(6);
+  }
+  // the caller's stream completes after every lane
+  for (int li = 1; li < NS; ++li) {
+    cudaEvent_t e;
+    PGSVT_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PGSVT_CK(cudaEventRecord(e, lanes[li].s));
+    PGSVT_CK(cudaStreamWaitEvent(s, e, 0));
+    cudaEventDestroy(e);
   }
   unsigned long long cnt[4];
-  PGSVT_CK(cudaMemcpyAsync(cnt, d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  PGSVT_CK(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   PGSVT_CK(cudaStreamSynchronize(s));
   stats.d2h += sizeof(cnt);
   stats.evals += cnt[3];
+  stats.arps_exact += cnt[0];
+  stats.svd_sweeps += cnt[1];
+  stats.svd_fp64 += cnt[2];
+  clk0.accumulate(stats.stage);
+  for (auto& L : lanes) L.clk->accumulate(stats.stage);
   if (p.verbose)
-    std::fprintf(stderr, "pgsvt: %dx%dx%d, bs=%d, nwin=%d, patches=%d, batch=%d, "
+    std::fprintf(stderr, "pgsvt: %dx%dx%d, bs=%d, nwin=%d, patches=%d, batch=%d x %d streams, "
                          "arps fp64 steps=%llu, svd warp-sweeps=%llu, fp64 tests=%llu\n",
-                 S, S, nimg, g.bs, g.nwin, g.NP, W, cnt[0], cnt[1], cnt[2]);
+                 S, S, nimg, g.bs, g.nwin, g.NP, W, NS, cnt[0], cnt[1], cnt[2]);
 }
 
 template <typename Fn>
@@ -428,6 +574,13 @@ int guarded(pgsvt_status* st, Fn&& fn) {
     st->h2d_bytes = stats.h2d;
     st->d2h_bytes = stats.d2h;
     st->risk_evals = stats.evals;
+    st->windows = stats.windows;
+    for (int i = 0; i < 8; ++i) st->stage_seconds[i] = stats.stage[i];
+    st->svd_launches = stats.svd_launches;
+    st->svd_matrices = stats.svd_matrices;
+    st->arps_exact_steps = stats.arps_exact;
+    st->svd_fp64_tests = stats.svd_fp64;
+    st->svd_warp_sweeps = stats.svd_sweeps;
     st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::snprintf(st->message, sizeof(st->message), "%s", g_err.c_str());
   }
@@ -547,8 +700,10 @@ struct OneWindow {
     d.V0 = mem.arr<float>((size_t)g.NC * g.nwin * g.NP);
     d.sv = mem.arr<float>((size_t)4 * g.NC * g.NP);
     d.hv = mem.arr<float>((size_t)4 * g.NC * g.NP);
+    d.nlive0 = mem.arr<int32_t>(g.NP);
     PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * 4 * g.NC * g.NP, s));
-    d.acc = mem.arr<unsigned long long>((size_t)pb.K * g.cube());
+    pb.acc64 = 1;  // a caller-given trajectory table may stack any number of patches
+    d.acc = mem.get(sizeof(unsigned long long) * pb.K * g.cube());
     PGSVT_CK(cudaMemsetAsync(d.acc, 0, sizeof(unsigned long long) * pb.K * g.cube(), s));
     d.part_lin = mem.arr<double>((size_t)pb.K * d.nblk_eval);
     d.part_mse = mem.arr<double>(std::max<size_t>((size_t)pb.K * d.nblk_mse, 256));
@@ -587,6 +742,8 @@ int pgsvt_default_params(pgsvt_params* p) {
   p->window_batch = 0;
   p->lambda_hint = -1.0;
   p->hint_span = 2.0;
+  p->frame_begin = 0;
+  p->frame_end = 0;
   return PGSVT_OK;
 }
 
@@ -688,8 +845,13 @@ int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t bl
       std::vector<float> h((size_t)g.NC * g.NP);
       PGSVT_CK(cudaMemcpyAsync(h.data(), ow.d.sv, h.size() * 4, cudaMemcpyDeviceToHost, ow.s));
       PGSVT_CK(cudaStreamSynchronize(ow.s));
-      for (int pi = 0; pi < g.NP; ++pi)
-        for (int i = 0; i < g.nwin; ++i) S[(size_t)pi * g.nwin + i] = h[(size_t)i * g.NP + pi];
+      // back to the reference's patch order (sorted position index)
+      const std::vector<int32_t>& so = ow.su.sorted;
+      for (int pi = 0; pi < g.NP; ++pi) {
+        const int32_t pos = ow.su.plist[pi];
+        const size_t out = std::lower_bound(so.begin(), so.end(), pos) - so.begin();
+        for (int i = 0; i < g.nwin; ++i) S[out * g.nwin + i] = h[(size_t)i * g.NP + pi];
+      }
     }
   });
 }
@@ -713,8 +875,8 @@ int pgsvt_reconstruct_window(const double* u, uint32_t nrows, uint32_t nwin, uin
     ow.alloc_factors(1);
     PGSVT_CK(cudaMemsetAsync(ow.d.cnt, 0, sizeof(int32_t) * g.cube(), ow.s));
     PGSVT_CK(launch_fields(ow.pb, ow.d, ow.s));
-    PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
     PGSVT_CK(launch_search_init(ow.pb, ow.d, ow.s));
+    PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
     PGSVT_CK(launch_eval_round(ow.pb, ow.d, 2, ow.s));
     double* vd = ow.mem.arr<double>(g.cube());
     PGSVT_CK(launch_cube_out(ow.pb, ow.d, vd, ow.s));
@@ -762,6 +924,12 @@ int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t b
     ow.d.d2code = d2;
     ow.d.probe_stride = 0;
     PGSVT_CK(launch_fields(ow.pb, ow.d, ow.s));
+    {  // the largest requested lambda bounds the thresholds the SVD must keep
+      double upper = 0.0;
+      for (uint32_t j = 0; j < nl; ++j) upper = std::max(upper, lambdas[j]);
+      PGSVT_CK(cudaMemcpyAsync(&ow.d.wc->upper, &upper, sizeof(double), cudaMemcpyHostToDevice, ow.s));
+      PGSVT_CK(cudaStreamSynchronize(ow.s));
+    }
     PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
     double* out = ow.mem.arr<double>(kMaxK);
     for (uint32_t j0 = 0; j0 < nl; j0 += kMaxK) {

@@ -15,8 +15,9 @@
 // the SVD epilogue stores h_i = u_i^T G_p v_i once, and a lambda evaluation
 // needs only sum_i g_i(lambda) h_i per patch and copy.  Only sum (Uh-U)^2 needs
 // the clean reconstruction voxel by voxel: copy 0 is rebuilt and scattered
-// into a fixed-point (2^-32) int64 accumulator, which makes the sums
-// independent of the order of the atomics, so the whole search is
+// into a fixed-point accumulator (int32 at 2^-20, or int64 at 2^-32 when one
+// voxel can collect every patch, as with the zero-motion quirk), which makes
+// the sums independent of the order of the atomics, so the whole search is
 // deterministic.
 #include <algorithm>
 
@@ -248,11 +249,43 @@ __global__ void k_search_step(Problem pb, DeviceBuffers d) {
   s.nnext = s.K;
 }
 
+// ---- fixed-point accumulators
+template <typename T>
+struct Acc;
+template <>
+struct Acc<int> {  // 2^-20: one voxel holds |sum| < 2048
+  static constexpr float kScale = 1048576.f;
+  __device__ static int fix(float v) { return __float2int_rn(v * kScale); }
+  __device__ static float unfix(int a) { return (float)a * (1.f / kScale); }
+  __device__ static int from_tile(int t) { return t; }
+  __device__ static void add(int* p, int v) { atomicAdd(p, v); }
+};
+template <>
+struct Acc<unsigned long long> {  // 2^-32
+  __device__ static long long fix(float v) { return fix32(v); }
+  __device__ static float unfix(unsigned long long a) { return unfix32((long long)a); }
+  __device__ static long long from_tile(int t) { return (long long)t * 4096; }
+  __device__ static void add(unsigned long long* p, long long v) {
+    atomicAdd(p, (unsigned long long)v);
+  }
+};
+
 // ---- one evaluation round: shrink, linear terms, rebuild + scatter of copy 0
 //
-// Block = 32 consecutive kept patches x nwin warps; warp k rebuilds column k
-// (trajectory slice k) of its lanes' patches.
-template <int BS>
+// Block = 32 kept patches (an 8 x 4 tile of grid positions, see the patch
+// order in capi.cu) x nwin warps.  Phase A spreads the (lambda, copy) pairs
+// over all warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0
+// go to shared memory and sum_i g_i h_i of every copy to per-lane partials.
+// Phase B: warp k rebuilds column k (trajectory slice k) of its lanes'
+// patches from the live singular triplets.  The 32 rebuilt blocks of one
+// slice overlap heavily, so each warp sums them into a shared-memory tile in
+// int32 fixed point (2^-20, order-free) and adds the tile to the accumulator
+// with one atomic per touched pixel.
+
+constexpr int kTileMax = 512;      // pixels of a warp's shared-memory tile
+constexpr float kTileBound = 60.f; // |value| above this bypasses the tile
+
+template <int BS, typename AccT>
 __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   constexpr int M = BS * BS;
   const Geometry& g = pb.g;
@@ -261,58 +294,82 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   const int nl = final_pass ? 1 : st.nnext;
   if (!final_pass && (st.done || nl == 0)) return;
   const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
   const int p = blockIdx.x * 32 + lane;
   const bool live = p < g.NP;
   const int NC = g.NC;
   const size_t NP = g.NP;
-  extern __shared__ float sg[];             // [nl][NC][32]
+  const bool lin_terms = pb.optimize && !final_pass;
+  const int ncp = lin_terms ? d.ncopies : 1;
+  extern __shared__ float sg[];  // g of copy 0 [nl][NC][32], lin [nl][4][32], tiles
+  float* slin = sg + (size_t)nl * NC * 32;
+  int* tiles = (int*)(slin + (size_t)nl * 4 * 32);
   __shared__ int srmax[kMaxK];
   const WinConst& wc = d.wc[w];
-  const int ncp = d.ncopies;
-  // phase A: warp j < nl computes g for lambda j
-  for (int j = k; j < nl; j += blockDim.x >> 5) {
-    const double lamd = final_pass ? st.final_lambda : st.next[j];
-    const float lam = (float)lamd;
+  int* tile = tiles + (size_t)k * kTileMax;
+  for (int i = lane; i < kTileMax; i += 32) tile[i] = 0;
+  // phase A
+  for (int task = k; task < nl * ncp; task += nwarps) {
+    const int j = task / ncp, c = task % ncp;
+    const float lam = (float)(final_pass ? st.final_lambda : st.next[j]);
+    const float* sv = d.sv + ((size_t)w * 4 + c) * NC * NP;
+    const float* hv = d.hv + ((size_t)w * 4 + c) * NC * NP;
+    const float smax = live ? sv[p] : 0.f;  // sorted: column 0 is the largest
     float lin = 0.f;
     int r0 = 0;
-    for (int c = 0; c < 4; ++c) {
-      if (c >= ncp && !(c == 3 && ncp == 4)) continue;
-      if (c > 0 && (final_pass || !pb.optimize)) break;
-      const float* sv = d.sv + ((size_t)w * 4 + c) * NC * NP;
-      const float* hv = d.hv + ((size_t)w * 4 + c) * NC * NP;
-      const float smax = live ? sv[p] : 0.f;  // sorted: column 0 is the largest
-      for (int i = 0; i < NC; ++i) {
-        const float s = live ? sv[(size_t)i * NP + p] : 0.f;
-        float th;
-        if (pb.expw) th = fabsf(smax * expf(-0.5f * lam * (s * s)));  // svt.hpp:137
-        else th = lam;                                                // svt.hpp:142
-        const float gi = fmaxf(fabsf(s) - th, 0.f);
-        if (c == 0) {
-          sg[((size_t)j * NC + i) * 32 + lane] = gi;
-          r0 += gi > 0.f;
-        }
-        if (pb.optimize && !final_pass && live) lin = fmaf(gi, hv[(size_t)i * NP + p], lin);
+    for (int i = 0; i < NC; ++i) {
+      const float s = live ? sv[(size_t)i * NP + p] : 0.f;
+      float th;
+      if (pb.expw) th = fabsf(smax * expf(-0.5f * lam * (s * s)));  // svt.hpp:137
+      else th = lam;                                                // svt.hpp:142
+      const float gi = fmaxf(fabsf(s) - th, 0.f);
+      if (c == 0) {
+        sg[((size_t)j * NC + i) * 32 + lane] = gi;
+        r0 += gi > 0.f;
       }
+      if (lin_terms && live) lin = fmaf(gi, hv[(size_t)i * NP + p], lin);
     }
-    if (!final_pass && pb.optimize) {
+    slin[((size_t)j * 4 + c) * 32 + lane] = lin;
+    if (c == 0) {
+      for (int o = 16; o > 0; o >>= 1) r0 = max(r0, __shfl_xor_sync(0xffffffffu, r0, o));
+      if (lane == 0) srmax[j] = r0;
+    }
+  }
+  __syncthreads();
+  if (lin_terms)
+    for (int j = k; j < nl; j += nwarps) {
+      float lin = 0.f;
+      for (int c = 0; c < ncp; ++c) lin += slin[((size_t)j * 4 + c) * 32 + lane];
       const double t = warp_sum_d((double)lin);
       if (lane == 0) d.part_lin[((size_t)w * pb.K + j) * d.nblk_eval + blockIdx.x] = t;
     }
-    for (int o = 16; o > 0; o >>= 1) r0 = max(r0, __shfl_xor_sync(0xffffffffu, r0, o));
-    if (lane == 0) srmax[j] = r0;
-  }
-  __syncthreads();
-  if (!live || k >= g.nwin) return;
+  if (k >= g.nwin) return;
   if (final_pass == 1 && k != wc.out_slice) return;  // 2: every slice
-  const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
-  const int y = pc & 0xffffu, x = pc >> 16;
+  int y = 0, x = 0;
+  if (live) {
+    const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
+    y = pc & 0xffffu;
+    x = pc >> 16;
+  }
+  // the warp's footprint in this slice
+  int y0 = live ? y : 1 << 30, y1 = live ? y : -1, x0 = live ? x : 1 << 30, x1 = live ? x : -1;
+  for (int o = 16; o > 0; o >>= 1) {
+    y0 = min(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    y1 = max(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+  }
+  const int th = y1 - y0 + BS, tw = x1 - x0 + BS;
+  const bool use_tile = (y1 >= 0) && th * tw <= kTileMax;
+  const int nlive = live ? d.nlive0[(size_t)w * NP + p] : 0;
   const float* U0 = d.U0 + (size_t)w * NC * M * NP;
   const float* V0 = d.V0 + (size_t)w * NC * g.nwin * NP;
+  AccT* accw = (AccT*)d.acc;
   float col[M];
   for (int j = 0; j < nl; ++j) {
 #pragma unroll
     for (int e = 0; e < M; ++e) col[e] = 0.f;
-    const int rm = srmax[j];
+    const int rm = min(srmax[j], nlive);
     for (int i = 0; i < rm; ++i) {
       const float coef = sg[((size_t)j * NC + i) * 32 + lane] * V0[((size_t)i * g.nwin + k) * NP + p];
       if (coef == 0.f) continue;
@@ -320,67 +377,111 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
 #pragma unroll
       for (int e = 0; e < M; ++e) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
     }
-    unsigned long long* acc = d.acc + (((size_t)w * pb.K + j) * g.nwin + k) * g.F();
+    AccT* acc = accw + (((size_t)w * pb.K + j) * g.nwin + k) * g.F();
+    if (use_tile) {
+      if (live) {
 #pragma unroll
-    for (int e = 0; e < M; ++e) {
-      const long long q = __float2ll_rn(col[e] * 4294967296.0f);
-      if (q != 0) atomicAdd(acc + (y + e % BS) + (size_t)(x + e / BS) * g.S, (unsigned long long)q);
+        for (int e = 0; e < M; ++e) {
+          const float v = col[e];
+          if (v == 0.f) continue;
+          if (fabsf(v) <= kTileBound)
+            atomicAdd(tile + (y - y0 + e % BS) + (x - x0 + e / BS) * th, __float2int_rn(v * 1048576.f));
+          else
+            Acc<AccT>::add(acc + (y + e % BS) + (size_t)(x + e / BS) * g.S, Acc<AccT>::fix(v));
+        }
+      }
+      __syncwarp();
+      for (int t = lane; t < th * tw; t += 32) {
+        const int v = tile[t];
+        if (v != 0) {
+          tile[t] = 0;
+          Acc<AccT>::add(acc + (y0 + t % th) + (size_t)(x0 + t / th) * g.S, Acc<AccT>::from_tile(v));
+        }
+      }
+      __syncwarp();
+    } else if (live) {
+#pragma unroll
+      for (int e = 0; e < M; ++e) {
+        const auto q = Acc<AccT>::fix(col[e]);
+        if (q != 0) Acc<AccT>::add(acc + (y + e % BS) + (size_t)(x + e / BS) * g.S, q);
+      }
     }
   }
 }
 
-// ---- sum over voxels of (Uh - U)^2 for each lambda of the round; clears acc
+// ---- sum over voxels of (Uh - U)^2 for every lambda of the round; clears acc
+template <typename AccT>
 __global__ void k_mse(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
-  const int w = blockIdx.z, j = blockIdx.y;
+  const int w = blockIdx.y;
   const SearchState& st = d.st[w];
-  if (st.done || j >= st.nnext) return;
+  if (st.done || st.nnext == 0) return;
+  const int nl = st.nnext;
   const size_t C = g.cube();
   const float* u = d.u + (size_t)w * C;
   const int32_t* cnt = d.cnt + (size_t)w * C;
-  unsigned long long* acc = d.acc + ((size_t)w * pb.K + j) * C;
-  double tot = 0.0;
-  for (size_t i0 = blockIdx.x * (size_t)blockDim.x * 4 + threadIdx.x; i0 < C;
-       i0 += (size_t)gridDim.x * blockDim.x * 4) {
-    float part = 0.f;
+  AccT* acc = (AccT*)d.acc + (size_t)w * pb.K * C;
+  double tot[kMaxK];
+  float part[kMaxK];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const size_t i = i0 + (size_t)q * blockDim.x;
-      if (i >= C) break;
-      const long long a = (long long)acc[i];
-      acc[i] = 0ull;
-      const int n = cnt[i];
-      const float uh = n > 0 ? (float)((double)a * (1.0 / 4294967296.0)) / (float)n : 0.f;
-      const float df = uh - u[i];
-      part = fmaf(df, df, part);
+  for (int j = 0; j < kMaxK; ++j) tot[j] = 0.0;
+  int n8 = 0;
+#pragma unroll
+  for (int j = 0; j < kMaxK; ++j) part[j] = 0.f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < C;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int n = __ldg(cnt + i);
+    const float uv = __ldg(u + i);
+    const float inv = n > 0 ? 1.f / (float)n : 0.f;
+#pragma unroll
+    for (int j = 0; j < kMaxK; ++j) {
+      if (j >= nl) break;
+      const AccT a = acc[(size_t)j * C + i];
+      acc[(size_t)j * C + i] = 0;
+      const float df = Acc<AccT>::unfix(a) * inv - uv;
+      part[j] = fmaf(df, df, part[j]);
     }
-    tot += part;
+    if (++n8 == 8) {  // FP32 partials over 8 voxels, FP64 beyond
+      n8 = 0;
+#pragma unroll
+      for (int j = 0; j < kMaxK; ++j) {
+        tot[j] += part[j];
+        part[j] = 0.f;
+      }
+    }
   }
-  tot = warp_sum_d(tot);
-  __shared__ double sm[32];
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = tot;
+  __shared__ double sm[kMaxK][8];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < kMaxK; ++j) {
+    if (j >= nl) break;
+    const double t = warp_sum_d(tot[j] + part[j]);
+    if (lane == 0) sm[j][wid] = t;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < nl) {
+    const int j = threadIdx.x;
     double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sm[q];
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sm[j][q];
     d.part_mse[((size_t)w * pb.K + j) * d.nblk_mse + blockIdx.x] = t;
   }
 }
 
 // ---- output slice and estimates (pguresvt.hpp:146-166)
+template <typename AccT>
 __global__ void k_output(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
   const int w = blockIdx.y;
   const WinConst& wc = d.wc[w];
   const size_t F = g.F();
-  const size_t off = ((size_t)w * pb.K * g.nwin + wc.out_slice) * F;
+  AccT* acc = (AccT*)d.acc + ((size_t)w * pb.K * g.nwin + wc.out_slice) * F;
   const int32_t* cnt = d.cnt + (size_t)w * g.cube() + (size_t)wc.out_slice * F;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < F;
        i += (size_t)gridDim.x * blockDim.x) {
-    const long long a = (long long)d.acc[off + i];
-    d.acc[off + i] = 0ull;
+    const AccT a = acc[i];
+    acc[i] = 0;
     const int n = cnt[i];
-    double v = n > 0 ? ((double)a * (1.0 / 4294967296.0)) / n : 0.0;
+    double v = n > 0 ? (double)Acc<AccT>::unfix(a) / n : 0.0;
     if (!isfinite(v)) v = 0.0;
     d.Y[(size_t)wc.t * F + i] = v * wc.umax;
   }
@@ -394,15 +495,17 @@ __global__ void k_output(Problem pb, DeviceBuffers d) {
 }
 
 // ---- whole reconstructed window v = acc / cnt (svt.hpp:163-164), window 0
+template <typename AccT>
 __global__ void k_cube_out(Problem pb, DeviceBuffers d, double* v) {
   const Geometry& g = pb.g;
   const size_t C = g.cube();
+  AccT* acc = (AccT*)d.acc;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < C;
        i += (size_t)gridDim.x * blockDim.x) {
-    const long long a = (long long)d.acc[i];
-    d.acc[i] = 0ull;
+    const AccT a = acc[i];
+    acc[i] = 0;
     const int n = d.cnt[i];
-    double q = n > 0 ? ((double)a * (1.0 / 4294967296.0)) / n : 0.0;
+    double q = n > 0 ? (double)Acc<AccT>::unfix(a) / n : 0.0;
     v[i] = isfinite(q) ? q : 0.0;
   }
 }
@@ -426,17 +529,44 @@ __global__ void k_risk_collect(Problem pb, DeviceBuffers d, double* out) {
   }
 }
 
-template <typename... A>
-void launch_k_eval(int bs, dim3 grid, int threads, size_t shm, cudaStream_t s, A... a) {
+size_t eval_smem(const Geometry& g, int nl) {
+  return (size_t)nl * (g.NC + 4) * 32 * sizeof(float) + (size_t)g.nwin * kTileMax * sizeof(int);
+}
+
+template <int BS, typename AccT>
+void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const Problem& pb,
+                      const DeviceBuffers& d, int final_pass) {
+  cudaFuncSetAttribute(k_eval<BS, AccT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass);
+}
+
+template <typename AccT>
+void launch_k_eval_t(int bs, dim3 grid, int threads, size_t shm, cudaStream_t s,
+                     const Problem& pb, const DeviceBuffers& d, int final_pass) {
   switch (bs) {
-    case 2: k_eval<2><<<grid, threads, shm, s>>>(a...); break;
-    case 3: k_eval<3><<<grid, threads, shm, s>>>(a...); break;
-    case 4: k_eval<4><<<grid, threads, shm, s>>>(a...); break;
-    case 5: k_eval<5><<<grid, threads, shm, s>>>(a...); break;
-    case 6: k_eval<6><<<grid, threads, shm, s>>>(a...); break;
-    case 7: k_eval<7><<<grid, threads, shm, s>>>(a...); break;
-    default: k_eval<8><<<grid, threads, shm, s>>>(a...); break;
+    case 2: launch_k_eval_bs<2, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 3: launch_k_eval_bs<3, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 4: launch_k_eval_bs<4, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 5: launch_k_eval_bs<5, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 6: launch_k_eval_bs<6, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 7: launch_k_eval_bs<7, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    default: launch_k_eval_bs<8, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
   }
+}
+
+void launch_k_eval(const Problem& pb, const DeviceBuffers& d, int final_pass, int nl,
+                   cudaStream_t s) {
+  const Geometry& g = pb.g;
+  const size_t shm = eval_smem(g, nl);
+  const dim3 grid(d.nblk_eval, pb.W);
+  if (pb.acc64) launch_k_eval_t<unsigned long long>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass);
+  else launch_k_eval_t<int>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass);
+}
+
+void launch_k_mse(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+  const dim3 grid(d.nblk_mse, pb.W);
+  if (pb.acc64) k_mse<unsigned long long><<<grid, 256, 0, s>>>(pb, d);
+  else k_mse<int><<<grid, 256, 0, s>>>(pb, d);
 }
 
 }  // namespace
@@ -462,30 +592,24 @@ cudaError_t launch_search_init(const Problem& pb, const DeviceBuffers& d, cudaSt
 
 cudaError_t launch_eval_round(const Problem& pb, const DeviceBuffers& d, int final_pass,
                               cudaStream_t s) {
-  const Geometry& g = pb.g;
-  const int nl = final_pass ? 1 : pb.K;
-  const size_t shm = (size_t)nl * g.NC * 32 * sizeof(float);
-  dim3 ge(d.nblk_eval, pb.W);
-  launch_k_eval(g.bs, ge, 32 * g.nwin, shm, s, pb, d, final_pass);
+  launch_k_eval(pb, d, final_pass, final_pass ? 1 : pb.K, s);
   if (final_pass) return cudaGetLastError();
-  dim3 gm(d.nblk_mse, pb.K, pb.W);
-  k_mse<<<gm, 256, 0, s>>>(pb, d);
+  launch_k_mse(pb, d, s);
   k_search_step<<<(pb.W + 63) / 64, 64, 0, s>>>(pb, d);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cube_out(const Problem& pb, const DeviceBuffers& d, double* v,
                             cudaStream_t s) {
-  k_cube_out<<<512, 256, 0, s>>>(pb, d, v);
+  if (pb.acc64) k_cube_out<unsigned long long><<<512, 256, 0, s>>>(pb, d, v);
+  else k_cube_out<int><<<512, 256, 0, s>>>(pb, d, v);
   return cudaGetLastError();
 }
 
 cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double* out,
                               cudaStream_t s) {
-  const Geometry& g = pb.g;
-  const size_t shm = (size_t)pb.K * g.NC * 32 * sizeof(float);
-  launch_k_eval(g.bs, dim3(d.nblk_eval, 1), 32 * g.nwin, shm, s, pb, d, 0);
-  k_mse<<<dim3(d.nblk_mse, pb.K, 1), 256, 0, s>>>(pb, d);
+  launch_k_eval(pb, d, 0, pb.K, s);
+  launch_k_mse(pb, d, s);
   k_risk_collect<<<1, kMaxK, 0, s>>>(pb, d, out);
   return cudaGetLastError();
 }
@@ -493,7 +617,8 @@ cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double*
 cudaError_t launch_output(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   const Geometry& g = pb.g;
   dim3 go((unsigned)std::min<size_t>((g.F() + 255) / 256, 512), pb.W);
-  k_output<<<go, 256, 0, s>>>(pb, d);
+  if (pb.acc64) k_output<unsigned long long><<<go, 256, 0, s>>>(pb, d);
+  else k_output<int><<<go, 256, 0, s>>>(pb, d);
   return cudaGetLastError();
 }
 

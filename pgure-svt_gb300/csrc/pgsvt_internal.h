@@ -20,7 +20,8 @@
 //   sv,hv   f32 [W][4][NC][NP]    singular values and risk projections of
 //                                 copies 0 (clean), 1 (+eps2*delta2),
 //                                 2 (-eps2*delta2), 3 (+eps1*delta1)
-//   acc     i64 [W][K][nwin][S*S] fixed-point (2^-32) scatter accumulators
+//   acc     i32 [W][K][nwin][S*S] fixed-point (2^-20) scatter accumulators
+//           (i64 at 2^-32 when a voxel can collect every patch)
 // NP is the number of kept patches (svt.hpp:61-94), M = bs*bs, N = nwin,
 // NC = N rounded up to the kernel's even column count.
 #ifndef PGSVT_INTERNAL_H
@@ -35,6 +36,25 @@ constexpr int kMaxK = 16;          // lambda values per evaluation round
 constexpr int kMaxPts = 160;       // evaluated points kept per window
 constexpr int kMaxMW = 15;         // motion window supported by ARPS
 constexpr double kFixScale = 4294967296.0;  // 2^32 fixed-point scale
+
+// round(v * 2^32) toward zero as an int64, with integer instructions only
+// (float <-> 64-bit integer conversions run on the FP64 unit)
+__device__ __forceinline__ long long fix32(float v) {
+  const int b = __float_as_int(v);
+  const int ex = ((b >> 23) & 0xff) - 127;
+  if (ex < -33) return 0;  // |v| < 2^-33 (also +-0, denormals)
+  const long long m = (long long)((b & 0x7fffff) | 0x800000);
+  const int sh = ex + 9;   // v * 2^32 = m * 2^(ex - 23 + 32)
+  const long long r = sh >= 0 ? (m << sh) : (m >> (-sh));
+  return b < 0 ? -r : r;
+}
+
+// int64 fixed-point value (2^-32) to float, with 32-bit conversions only
+__device__ __forceinline__ float unfix32(long long a) {
+  const int hi = (int)(a >> 32);
+  const unsigned lo = (unsigned)(a & 0xffffffffll);
+  return (float)hi + (float)lo * 2.3283064365386963e-10f;
+}
 
 // Per-window constants, computed on the device.
 struct WinConst {
@@ -97,6 +117,7 @@ struct Problem {
   double tol;
   int max_evals, rounds;
   double hint, hint_span;
+  int acc64;             // accumulators int64 at 2^-32 (else int32 at 2^-20)
 };
 
 struct DeviceBuffers {
@@ -119,7 +140,8 @@ struct DeviceBuffers {
   float* V0;
   float* sv;
   float* hv;
-  unsigned long long* acc;
+  int32_t* nlive0;         // [W][NP] singular triplets of copy 0 that can survive
+  void* acc;               // [W][K][nwin][S*S] int32 or int64 fixed point
   double* part_lin;        // [W][K][nblk_eval]
   double* part_mse;        // [W][K][nblk_mse]
   WinConst* wc;

@@ -45,31 +45,34 @@ def _drift(rng, nt, max_step, integer):
 
 def blobs(side, nt, nblobs, seed, max_step=1.0, integer_drift=True, lattice=False,
           background=5.0):
-    """Clean (side, side, nt) float64 sequence, column-major like the reference."""
+    """Clean (side, side, nt) float64 sequence, column-major like the reference.
+
+    Isotropic Gaussians are separable, so a frame is background +
+    Gy diag(peak) Gx^T with Gy[y, b] = exp(-(y - cy_b)^2 / 2s_b^2) (same for x).
+    """
     rng = np.random.default_rng(seed)
     cy = rng.uniform(0, side, nblobs)
     cx = rng.uniform(0, side, nblobs)
     sg = rng.uniform(2.0, 6.0, nblobs)
     pk = rng.uniform(20.0, 200.0, nblobs)
     off = _drift(rng, nt, max_step, integer_drift)
-    yy = np.arange(side, dtype=float)[:, None]
-    xx = np.arange(side, dtype=float)[None, :]
+    r = np.arange(side, dtype=float)[:, None]
     X = np.empty((side, side, nt), dtype=float, order="F")
     if lattice:
         period = rng.uniform(6.0, 10.0, 2)
         phase = rng.uniform(0, 2 * np.pi, 2)
     for t in range(nt):
         dy, dx = off[t]
-        f = np.full((side, side), background)
-        for b in range(nblobs):
-            f += pk[b] * np.exp(-((yy - cy[b] - dy) ** 2 + (xx - cx[b] - dx) ** 2) / (2 * sg[b] ** 2))
-        X[:, :, t] = f
+        gy = np.exp(-((r - cy[None, :] - dy) ** 2) / (2 * sg[None, :] ** 2))
+        gx = np.exp(-((r - cx[None, :] - dx) ** 2) / (2 * sg[None, :] ** 2))
+        X[:, :, t] = background + gy @ (pk[:, None] * gx.T)
     if lattice:
         amp = 0.15 * X.mean()
         for t in range(nt):
             dy, dx = off[t]
-            X[:, :, t] += amp * (np.sin(2 * np.pi * (yy - dy) / period[0] + phase[0])
-                                 * np.sin(2 * np.pi * (xx - dx) / period[1] + phase[1]))
+            ly = np.sin(2 * np.pi * (r[:, 0] - dy) / period[0] + phase[0])
+            lx = np.sin(2 * np.pi * (r[:, 0] - dx) / period[1] + phase[1])
+            X[:, :, t] += amp * np.outer(ly, lx)
         np.maximum(X, 0.0, out=X)
     return X
 
