@@ -107,17 +107,17 @@ std::vector<int32_t> patch_list(int S, int bs, int ov) {
   return std::vector<int32_t>(v.begin(), v.end());
 }
 
-// Processing order of the kept patches: 8 x 4 tiles of grid positions (rows
-// fastest), so the 32 patches of a warp cover a compact region of every slice
-// and their rebuilt blocks overlap (k_eval).  The order has no effect on the
-// results: the overlap sums are integer sums.
+// Processing order of the kept patches: 8 x 8 tiles of grid positions (rows
+// fastest), so the 64 patches of a lambda-evaluation block cover a compact
+// region of every slice and their rebuilt blocks overlap (k_eval).  The
+// order has no effect on the results: the overlap sums are integer sums.
 std::vector<int32_t> tile_order(const std::vector<int32_t>& plist, int S, int bs) {
   const int n1 = S - bs + 1, ti = (n1 + 7) / 8;
   std::vector<std::pair<int64_t, int32_t>> key;
   key.reserve(plist.size());
   for (int32_t it : plist) {
     const int i = it % n1, j = it / n1;
-    const int64_t tk = ((int64_t)(j / 4) * ti + i / 8) * 32 + (j % 4) * 8 + (i % 8);
+    const int64_t tk = ((int64_t)(j / 8) * ti + i / 8) * 64 + (j % 8) * 8 + (i % 8);
     key.push_back({tk, it});
   }
   std::sort(key.begin(), key.end());

@@ -27,8 +27,6 @@ namespace pgsvt {
 
 namespace {
 
-constexpr int kMseBlocks = 128;
-
 __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -181,26 +179,44 @@ __device__ void search_finish(SearchState& s, unsigned long long* counters) {
   s.nnext = 0;
 }
 
+// Risk of lambda slot j of window w (pgure.hpp:136) from the block
+// partials, reduced by the calling block in a fixed order.
+__device__ double block_sum(const double* v, int n, double* red) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += v[i];
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
 // Merge the risks of the pending round and schedule the next one.
-__global__ void k_search_step(Problem pb, DeviceBuffers d) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= pb.W) return;
+// One block per window: the partial sums are reduced in parallel, thread 0
+// advances the search state.
+__global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d) {
+  const int w = blockIdx.x;
   SearchState& s = d.st[w];
   if (s.done) return;
+  __shared__ double red[256];
+  __shared__ double risk[kMaxK];
   const Geometry& g = pb.g;
   const WinConst& wc = d.wc[w];
   const double N = (double)g.S * g.S * g.nwin;
   const double a = wc.alpha, m = wc.mu, s2 = wc.sigma * wc.sigma;
-  const int nbe = d.nblk_eval, nbm = d.nblk_mse;
+  const int nn = s.nnext;
+  for (int j = 0; j < nn; ++j) {
+    const double lin = block_sum(d.part_lin + ((size_t)w * pb.K + j) * d.nblk_eval, d.nblk_eval, red);
+    const double mse = block_sum(d.part_mse + ((size_t)w * pb.K + j) * d.nblk_mse, d.nblk_mse, red);
+    if (threadIdx.x == 0) risk[j] = (1.0 / N) * (mse + lin - (a + m) * wc.sum_u + m) - s2;  // pgure.hpp:136
+  }
+  if (threadIdx.x != 0) return;
   const double prev_best = s.npts > 0 ? s.risk[s.best] : 0.0;
-  for (int j = 0; j < s.nnext; ++j) {
-    double lin = 0.0, mse = 0.0;
-    const double* pl = d.part_lin + ((size_t)w * pb.K + j) * nbe;
-    const double* pm = d.part_mse + ((size_t)w * pb.K + j) * nbm;
-    for (int b = 0; b < nbe; ++b) lin += pl[b];
-    for (int b = 0; b < nbm; ++b) mse += pm[b];
-    // pgure.hpp:136
-    const double r = (1.0 / N) * (mse + lin - (a + m) * wc.sum_u + m) - s2;
+  for (int j = 0; j < nn; ++j) {
     int pos = s.npts;  // keep lambda ascending, new points after equal ones
     while (pos > 0 && s.lam[pos - 1] > s.next[j]) {
       s.lam[pos] = s.lam[pos - 1];
@@ -208,7 +224,7 @@ __global__ void k_search_step(Problem pb, DeviceBuffers d) {
       --pos;
     }
     s.lam[pos] = s.next[j];
-    s.risk[pos] = r;
+    s.risk[pos] = risk[j];
     ++s.npts;
   }
   s.evals_phase += s.nnext;
@@ -272,8 +288,8 @@ struct Acc<unsigned long long> {  // 2^-32
 
 // ---- one evaluation round: shrink, linear terms, rebuild + scatter of copy 0
 //
-// Block = 32 kept patches (an 8 x 4 tile of grid positions, see the patch
-// order in capi.cu) x nwin warps.  Phase A spreads the (lambda, copy) pairs
+// Block = 64 kept patches (an 8 x 8 tile of grid positions, see the patch
+// order in capi.cu; two per lane) x nwin warps.  Phase A spreads the (lambda, copy) pairs
 // over all warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0
 // go to shared memory and sum_i g_i h_i of every copy to per-lane partials.
 // Phase B: warp k rebuilds column k (trajectory slice k) of its lanes'
@@ -282,12 +298,13 @@ struct Acc<unsigned long long> {  // 2^-32
 // int32 fixed point (2^-20, order-free) and adds the tile to the accumulator
 // with one atomic per touched pixel.
 
-constexpr int kTileMax = 512;      // pixels of a warp's shared-memory tile
-constexpr float kTileBound = 60.f; // |value| above this bypasses the tile
+constexpr int kTileMax = 1024;     // pixels of a warp's shared-memory tile
+constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x 30 < 2048)
 
 template <int BS, typename AccT>
-__global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
+__global__ void __launch_bounds__(32 * 21) k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   constexpr int M = BS * BS;
+  constexpr int PB = kEvalPatches;  // patches per block
   const Geometry& g = pb.g;
   const int w = blockIdx.y;
   const SearchState& st = d.st[w];
@@ -295,22 +312,26 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   if (!final_pass && (st.done || nl == 0)) return;
   const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
-  const int p = blockIdx.x * 32 + lane;
-  const bool live = p < g.NP;
   const int NC = g.NC;
   const size_t NP = g.NP;
   const bool lin_terms = pb.optimize && !final_pass;
   const int ncp = lin_terms ? d.ncopies : 1;
-  extern __shared__ float sg[];  // g of copy 0 [nl][NC][32], lin [nl][4][32], tiles
-  float* slin = sg + (size_t)nl * NC * 32;
-  int* tiles = (int*)(slin + (size_t)nl * 4 * 32);
+  extern __shared__ float sg[];  // g of copy 0 [nl][NC][PB], lin [nl][4][PB], tiles
+  float* slin = sg + (size_t)nl * NC * PB;
+  int* tiles = (int*)(slin + (size_t)nl * 4 * PB);
   __shared__ int srmax[kMaxK];
   const WinConst& wc = d.wc[w];
   int* tile = tiles + (size_t)k * kTileMax;
   for (int i = lane; i < kTileMax; i += 32) tile[i] = 0;
-  // phase A
-  for (int task = k; task < nl * ncp; task += nwarps) {
-    const int j = task / ncp, c = task % ncp;
+  if (threadIdx.x < kMaxK) srmax[threadIdx.x] = 0;
+  __syncthreads();
+  // phase A: (lambda, copy, half) tasks over all warps
+  for (int task = k; task < nl * ncp * 2; task += nwarps) {
+    const int h = task & 1, jc = task >> 1;
+    const int j = jc / ncp, c = jc % ncp;
+    const int slot = h * 32 + lane;
+    const int p = blockIdx.x * PB + slot;
+    const bool live = p < g.NP;
     const float lam = (float)(final_pass ? st.final_lambda : st.next[j]);
     const float* sv = d.sv + ((size_t)w * 4 + c) * NC * NP;
     const float* hv = d.hv + ((size_t)w * 4 + c) * NC * NP;
@@ -324,35 +345,48 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
       else th = lam;                                                // svt.hpp:142
       const float gi = fmaxf(fabsf(s) - th, 0.f);
       if (c == 0) {
-        sg[((size_t)j * NC + i) * 32 + lane] = gi;
+        sg[((size_t)j * NC + i) * PB + slot] = gi;
         r0 += gi > 0.f;
       }
       if (lin_terms && live) lin = fmaf(gi, hv[(size_t)i * NP + p], lin);
     }
-    slin[((size_t)j * 4 + c) * 32 + lane] = lin;
+    slin[((size_t)j * 4 + c) * PB + slot] = lin;
     if (c == 0) {
       for (int o = 16; o > 0; o >>= 1) r0 = max(r0, __shfl_xor_sync(0xffffffffu, r0, o));
-      if (lane == 0) srmax[j] = r0;
+      if (lane == 0) atomicMax(&srmax[j], r0);
     }
   }
   __syncthreads();
   if (lin_terms)
     for (int j = k; j < nl; j += nwarps) {
       float lin = 0.f;
-      for (int c = 0; c < ncp; ++c) lin += slin[((size_t)j * 4 + c) * 32 + lane];
+      for (int h = 0; h < 2; ++h)
+        for (int c = 0; c < ncp; ++c) lin += slin[((size_t)j * 4 + c) * PB + h * 32 + lane];
       const double t = warp_sum_d((double)lin);
       if (lane == 0) d.part_lin[((size_t)w * pb.K + j) * d.nblk_eval + blockIdx.x] = t;
     }
   if (k >= g.nwin) return;
   if (final_pass == 1 && k != wc.out_slice) return;  // 2: every slice
-  int y = 0, x = 0;
-  if (live) {
-    const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
-    y = pc & 0xffffu;
-    x = pc >> 16;
+  int y[2], x[2], nlive[2];
+  bool live[2];
+  int y0 = 1 << 30, y1 = -1, x0 = 1 << 30, x1 = -1;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int p = blockIdx.x * PB + h * 32 + lane;
+    live[h] = p < g.NP;
+    y[h] = x[h] = nlive[h] = 0;
+    if (live[h]) {
+      const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
+      y[h] = pc & 0xffffu;
+      x[h] = pc >> 16;
+      nlive[h] = d.nlive0[(size_t)w * NP + p];
+      y0 = min(y0, y[h]);
+      y1 = max(y1, y[h]);
+      x0 = min(x0, x[h]);
+      x1 = max(x1, x[h]);
+    }
   }
   // the warp's footprint in this slice
-  int y0 = live ? y : 1 << 30, y1 = live ? y : -1, x0 = live ? x : 1 << 30, x1 = live ? x : -1;
   for (int o = 16; o > 0; o >>= 1) {
     y0 = min(y0, __shfl_xor_sync(0xffffffffu, y0, o));
     y1 = max(y1, __shfl_xor_sync(0xffffffffu, y1, o));
@@ -361,35 +395,45 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   }
   const int th = y1 - y0 + BS, tw = x1 - x0 + BS;
   const bool use_tile = (y1 >= 0) && th * tw <= kTileMax;
-  const int nlive = live ? d.nlive0[(size_t)w * NP + p] : 0;
   const float* U0 = d.U0 + (size_t)w * NC * M * NP;
   const float* V0 = d.V0 + (size_t)w * NC * g.nwin * NP;
   AccT* accw = (AccT*)d.acc;
-  float col[M];
+  constexpr int CH = M < 16 ? M : 16;  // rows rebuilt per pass (bounds registers)
   for (int j = 0; j < nl; ++j) {
-#pragma unroll
-    for (int e = 0; e < M; ++e) col[e] = 0.f;
-    const int rm = min(srmax[j], nlive);
-    for (int i = 0; i < rm; ++i) {
-      const float coef = sg[((size_t)j * NC + i) * 32 + lane] * V0[((size_t)i * g.nwin + k) * NP + p];
-      if (coef == 0.f) continue;
-      const float* ui = U0 + (size_t)i * M * NP + p;
-#pragma unroll
-      for (int e = 0; e < M; ++e) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
-    }
     AccT* acc = accw + (((size_t)w * pb.K + j) * g.nwin + k) * g.F();
-    if (use_tile) {
-      if (live) {
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      if (!live[h]) continue;
+      const int p = blockIdx.x * PB + h * 32 + lane;
+      const int rm = min(srmax[j], nlive[h]);
+#pragma unroll 1
+      for (int e0 = 0; e0 < M; e0 += CH) {
+        float col[CH];
 #pragma unroll
-        for (int e = 0; e < M; ++e) {
+        for (int e = 0; e < CH; ++e) col[e] = 0.f;
+        for (int i = 0; i < rm; ++i) {
+          const float coef = sg[((size_t)j * NC + i) * PB + h * 32 + lane] *
+                             V0[((size_t)i * g.nwin + k) * NP + p];
+          if (coef == 0.f) continue;
+          const float* ui = U0 + ((size_t)i * M + e0) * NP + p;
+#pragma unroll
+          for (int e = 0; e < CH; ++e)
+            if (e0 + e < M) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
+        }
+#pragma unroll
+        for (int e = 0; e < CH; ++e) {
+          const int ee = e0 + e;
           const float v = col[e];
-          if (v == 0.f) continue;
-          if (fabsf(v) <= kTileBound)
-            atomicAdd(tile + (y - y0 + e % BS) + (x - x0 + e / BS) * th, __float2int_rn(v * 1048576.f));
+          if (ee >= M || v == 0.f) continue;
+          const int er = ee % BS, ec = ee / BS;
+          if (use_tile && fabsf(v) <= kTileBound)
+            atomicAdd(tile + (y[h] - y0 + er) + (x[h] - x0 + ec) * th, __float2int_rn(v * 1048576.f));
           else
-            Acc<AccT>::add(acc + (y + e % BS) + (size_t)(x + e / BS) * g.S, Acc<AccT>::fix(v));
+            Acc<AccT>::add(acc + (y[h] + er) + (size_t)(x[h] + ec) * g.S, Acc<AccT>::fix(v));
         }
       }
+    }
+    if (use_tile) {
       __syncwarp();
       for (int t = lane; t < th * tw; t += 32) {
         const int v = tile[t];
@@ -399,19 +443,13 @@ __global__ void k_eval(Problem pb, DeviceBuffers d, int final_pass) {
         }
       }
       __syncwarp();
-    } else if (live) {
-#pragma unroll
-      for (int e = 0; e < M; ++e) {
-        const auto q = Acc<AccT>::fix(col[e]);
-        if (q != 0) Acc<AccT>::add(acc + (y + e % BS) + (size_t)(x + e / BS) * g.S, q);
-      }
     }
   }
 }
 
 // ---- sum over voxels of (Uh - U)^2 for every lambda of the round; clears acc
-template <typename AccT>
-__global__ void k_mse(Problem pb, DeviceBuffers d) {
+template <typename AccT, int KT>
+__global__ void __launch_bounds__(256) k_mse(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
   const int w = blockIdx.y;
   const SearchState& st = d.st[w];
@@ -421,41 +459,32 @@ __global__ void k_mse(Problem pb, DeviceBuffers d) {
   const float* u = d.u + (size_t)w * C;
   const int32_t* cnt = d.cnt + (size_t)w * C;
   AccT* acc = (AccT*)d.acc + (size_t)w * pb.K * C;
-  double tot[kMaxK];
-  float part[kMaxK];
+  float part[KT];  // a thread sees about 16 voxels: FP32 partials, FP64 beyond
 #pragma unroll
-  for (int j = 0; j < kMaxK; ++j) tot[j] = 0.0;
-  int n8 = 0;
-#pragma unroll
-  for (int j = 0; j < kMaxK; ++j) part[j] = 0.f;
+  for (int j = 0; j < KT; ++j) part[j] = 0.f;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < C;
        i += (size_t)gridDim.x * blockDim.x) {
     const int n = __ldg(cnt + i);
     const float uv = __ldg(u + i);
     const float inv = n > 0 ? 1.f / (float)n : 0.f;
+    AccT av[KT];  // every load first: the clears below could alias them
 #pragma unroll
-    for (int j = 0; j < kMaxK; ++j) {
-      if (j >= nl) break;
-      const AccT a = acc[(size_t)j * C + i];
-      acc[(size_t)j * C + i] = 0;
-      const float df = Acc<AccT>::unfix(a) * inv - uv;
-      part[j] = fmaf(df, df, part[j]);
-    }
-    if (++n8 == 8) {  // FP32 partials over 8 voxels, FP64 beyond
-      n8 = 0;
+    for (int j = 0; j < KT; ++j) av[j] = (j < nl) ? __ldcs(acc + (size_t)j * C + i) : (AccT)0;
 #pragma unroll
-      for (int j = 0; j < kMaxK; ++j) {
-        tot[j] += part[j];
-        part[j] = 0.f;
-      }
+    for (int j = 0; j < KT; ++j)
+      if (j < nl) __stcs(acc + (size_t)j * C + i, (AccT)0);
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const float df = Acc<AccT>::unfix(av[j]) * inv - uv;
+      if (j < nl) part[j] = fmaf(df, df, part[j]);
     }
   }
-  __shared__ double sm[kMaxK][8];
+  __shared__ double sm[KT][8];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
-  for (int j = 0; j < kMaxK; ++j) {
+  for (int j = 0; j < KT; ++j) {
     if (j >= nl) break;
-    const double t = warp_sum_d(tot[j] + part[j]);
+    const double t = warp_sum_d((double)part[j]);
     if (lane == 0) sm[j][wid] = t;
   }
   __syncthreads();
@@ -530,7 +559,8 @@ __global__ void k_risk_collect(Problem pb, DeviceBuffers d, double* out) {
 }
 
 size_t eval_smem(const Geometry& g, int nl) {
-  return (size_t)nl * (g.NC + 4) * 32 * sizeof(float) + (size_t)g.nwin * kTileMax * sizeof(int);
+  return (size_t)nl * (g.NC + 4) * kEvalPatches * sizeof(float) +
+         (size_t)g.nwin * kTileMax * sizeof(int);
 }
 
 template <int BS, typename AccT>
@@ -565,14 +595,21 @@ void launch_k_eval(const Problem& pb, const DeviceBuffers& d, int final_pass, in
 
 void launch_k_mse(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   const dim3 grid(d.nblk_mse, pb.W);
-  if (pb.acc64) k_mse<unsigned long long><<<grid, 256, 0, s>>>(pb, d);
-  else k_mse<int><<<grid, 256, 0, s>>>(pb, d);
+  if (pb.K <= 8) {
+    if (pb.acc64) k_mse<unsigned long long, 8><<<grid, 256, 0, s>>>(pb, d);
+    else k_mse<int, 8><<<grid, 256, 0, s>>>(pb, d);
+  } else {
+    if (pb.acc64) k_mse<unsigned long long, kMaxK><<<grid, 256, 0, s>>>(pb, d);
+    else k_mse<int, kMaxK><<<grid, 256, 0, s>>>(pb, d);
+  }
 }
 
 }  // namespace
 
-int eval_blocks(const Geometry& g) { return (g.NP + 31) / 32; }
-int mse_blocks(const Geometry&) { return kMseBlocks; }
+int eval_blocks(const Geometry& g) { return (g.NP + kEvalPatches - 1) / kEvalPatches; }
+int mse_blocks(const Geometry& g) {
+  return (int)std::max<size_t>(32, std::min<size_t>(1024, g.cube() / 4096));
+}
 
 cudaError_t launch_fields(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   const Geometry& g = pb.g;
@@ -595,7 +632,7 @@ cudaError_t launch_eval_round(const Problem& pb, const DeviceBuffers& d, int fin
   launch_k_eval(pb, d, final_pass, final_pass ? 1 : pb.K, s);
   if (final_pass) return cudaGetLastError();
   launch_k_mse(pb, d, s);
-  k_search_step<<<(pb.W + 63) / 64, 64, 0, s>>>(pb, d);
+  k_search_step<<<pb.W, 256, 0, s>>>(pb, d);
   return cudaGetLastError();
 }
 

@@ -35,6 +35,7 @@ namespace pgsvt {
 constexpr int kMaxK = 16;          // lambda values per evaluation round
 constexpr int kMaxPts = 160;       // evaluated points kept per window
 constexpr int kMaxMW = 15;         // motion window supported by ARPS
+constexpr int kEvalPatches = 64;   // kept patches per lambda-evaluation block (8 x 8 tile)
 constexpr double kFixScale = 4294967296.0;  // 2^32 fixed-point scale
 
 // round(v * 2^32) toward zero as an int64, with integer instructions only
