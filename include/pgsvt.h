@@ -189,6 +189,33 @@ int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin,
                       double sigma, int64_t random_seed, uint32_t compat_flags,
                       const double* lambdas, uint32_t nl, double* risk);
 
+/* Singular values of one window without any device allocation.
+ *
+ * This entry point has no counterpart in the reference.  It serves callers
+ * that cannot allocate device memory while they work: acquisition loops that
+ * reserved their memory up front, code running under an allocator that owns
+ * the whole device, or processes that must avoid cudaMalloc/cudaFree because
+ * those calls synchronise the device.  Inputs and outputs are caller-owned
+ * device memory: u_dev is the normalised window (float, nrows x nrows x nwin,
+ * column-major), rows_dev/cols_dev the trajectory table (int32, nwin x P as in
+ * pgsvt_arps_window), S_dev receives npatch x nwin singular values (descending
+ * per patch, patches in the reference's sorted order; NULL: only *npatch is
+ * set).  Intermediates live in a fixed static device array (about 1 MB, held
+ * by every GPU that loads the library until the process exits), so windows
+ * are limited to nrows <= PGSVT_NOALLOC_MAX_SIDE, nwin <= PGSVT_NOALLOC_MAX_NWIN
+ * and block_size <= 4; larger ones are rejected with PGSVT_ERR_INVALID_ARG.
+ * The first call on a device looks up that device's copy of the array (make
+ * it before any stream capture).  All calls share the array and it keeps the
+ * previous call's contents: calls whose GPU work overlaps race, so serialise
+ * them.  Runs on `stream` (a cudaStream_t, NULL: default stream) and returns
+ * once the work has completed.  Calls no allocating routine.                */
+#define PGSVT_NOALLOC_MAX_SIDE 64
+#define PGSVT_NOALLOC_MAX_NWIN 15
+int pgsvt_svd_window_noalloc(const float* u_dev, uint32_t nrows, uint32_t nwin,
+                             uint32_t block_size, uint32_t block_overlap,
+                             const int32_t* rows_dev, const int32_t* cols_dev,
+                             float* S_dev, uint32_t* npatch, void* stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* pgsvt_last_error(void);
 

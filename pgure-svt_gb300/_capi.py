@@ -27,7 +27,10 @@ COMPAT_ALL = 0x7
 # every symbol include/pgsvt.h declares
 EXPORTS = ("pgsvt_default_params", "pgsvt_denoise", "pgsvt_denoise_device",
            "pgsvt_arps_window", "pgsvt_svd_window", "pgsvt_reconstruct_window",
-           "pgsvt_risk_window", "pgsvt_last_error", "pgsvt_version")
+           "pgsvt_risk_window", "pgsvt_svd_window_noalloc", "pgsvt_last_error",
+           "pgsvt_version")
+NOALLOC_MAX_SIDE = 64
+NOALLOC_MAX_NWIN = 15
 
 
 class Params(ctypes.Structure):
@@ -93,6 +96,7 @@ def load(path=LIB_PATH):
     L.pgsvt_reconstruct_window.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp, dbl, vp]
     L.pgsvt_risk_window.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp, dbl, dbl, dbl, i64,
                                     u32, vp, u32, vp]
+    L.pgsvt_svd_window_noalloc.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, P(u32), vp]
     L.pgsvt_last_error.restype = ctypes.c_char_p
     L.pgsvt_version.restype = ctypes.c_char_p
     for name in EXPORTS:

@@ -713,6 +713,10 @@ struct OneWindow {
 
 }  // namespace
 
+namespace pgsvt {
+void set_last_error(const std::string& m) { g_err = m; }
+}  // namespace pgsvt
+
 extern "C" {
 
 int pgsvt_default_params(pgsvt_params* p) {

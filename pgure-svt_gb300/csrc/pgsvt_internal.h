@@ -30,6 +30,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace pgsvt {
 
 constexpr int kMaxK = 16;          // lambda values per evaluation round
@@ -176,6 +178,9 @@ cudaError_t launch_cube_out(const Problem& pb, const DeviceBuffers& d, double* v
                             cudaStream_t s);
 cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double* out,
                               cudaStream_t s);
+
+// message returned by pgsvt_last_error() on the calling thread
+void set_last_error(const std::string& m);
 
 int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
