@@ -798,7 +798,11 @@ int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimage
     std::fill(Y, Y + F * nimages, 0.0);
     std::fill(est, est + (size_t)nimages * 4, 0.0);
     std::vector<uint32_t> evals(nimages, 0);
-    fan_out(nimages, p->n_jobs, [&](uint32_t t) {
+    uint32_t fb = p->frame_begin, fe = p->frame_end;  // output frames computed
+    if (fb == 0 && fe == 0) fe = nimages;
+    if (fb >= fe || fe > nimages) throw Fail(1, "bad frame range");
+    fan_out(fe - fb, p->n_jobs, [&](uint32_t k) {
+      const uint32_t t = fb + k;
       const WindowOut o = run_window(X, *p, pl, t, Y + (size_t)t * F);
       est[t] = o.lambda;  // pguresvt.hpp:150-153 (unswapped alpha, mu, sigma)
       est[t + nimages] = p->alpha;
@@ -807,7 +811,7 @@ int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimage
       evals[t] = o.evals;
     });
     if (rep) {
-      rep->windows = nimages;
+      rep->windows = fe - fb;
       rep->risk_evals = 0;
       for (uint32_t e : evals) rep->risk_evals += e;
       rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

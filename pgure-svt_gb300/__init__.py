@@ -4,7 +4,7 @@ The compute runs in libpgsvt.so (hand-written sm_103a CUDA behind the C ABI
 of include/pgsvt.h); this package holds its ctypes binding, the ``SVT``
 estimator with the reference's Python parameters, and synthetic workloads.
 """
-from . import _capi
+from . import _capi, shard, synth
 from ._capi import (COMPAT_ALL, COMPAT_INT_DELTA1, COMPAT_SWAP_MU_SIGMA, COMPAT_ZERO_MOTION,
                     PgsvtError)
 from .svt import SVT

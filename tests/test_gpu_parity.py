@@ -222,3 +222,15 @@ def test_all_zero_sequence(capi):
     X = np.zeros((16, 16, 16), np.float32)
     Y, _, _ = capi.denoise(X, capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1))
     assert np.all(Y == 0)
+
+
+def test_frame_range_shards_sum_to_full_run(capi, pkg, g):
+    kw = dict(median_size=-1, optimize_pgure=0, lambda_=0.1)
+    Y, _, _ = capi.denoise(g["X"], capi.default_params(**kw))
+    parts = []
+    for r in range(3):
+        b, e = pkg.shard.shard_frames(g["X"].shape[2], 3, r)
+        Yr, _, _ = capi.denoise(g["X"], capi.default_params(frame_begin=b, frame_end=e, **kw))
+        assert not Yr[:, :, :b].any() and not Yr[:, :, e:].any()
+        parts.append(Yr)
+    np.testing.assert_array_equal(sum(parts), Y)
