@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=200)
     ap.add_argument("--patch", type=int, default=4)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--hint", type=float, default=-1.0, help="lambda proposal (learned form)")
+    ap.add_argument("--hint", type=float, default=-1.0, help="fixed lambda proposal")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-lambda arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=0, help="patch stride of the CPU sample")
     return ap.parse_args()
@@ -107,10 +108,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(side, frames, seed):
+def make_workload(side, frames, seed, with_clean=False):
     pkg = entry.load_package()
     noisy, clean, (a, m, s) = pkg.synth.workload("lattice_512", seed=seed, side=side, nt=frames)
+    if with_clean:
+        return noisy, (a, m, s), clean
     return noisy, (a, m, s)
+
+
+def psnr(clean, y):
+    """PSNR (dB) of y against the clean sequence, peak = max(clean)."""
+    return float(10 * np.log10(clean.max() ** 2 / np.mean((clean - y) ** 2)))
 
 
 def svd_flops(m, n):
@@ -188,7 +196,7 @@ def main():
     pkg = entry.load_package()
     capi = pkg._capi
     capi.load()
-    noisy, (a, m, s) = make_workload(args.side, args.frames, args.seed + rank)
+    noisy, (a, m, s), clean = make_workload(args.side, args.frames, args.seed + rank, True)
     S, nimg = args.side, args.frames
     n = S * S * nimg
     p = params(capi, a, m, s, args.patch, args.hint)
@@ -197,11 +205,14 @@ def main():
     x = torch.from_numpy(np.ascontiguousarray(noisy.ravel(order="F"))).cuda()
     y = torch.empty(n, dtype=torch.float64, device="cuda")
     est = torch.empty(nimg * 4, dtype=torch.float64, device="cuda")
+    risk = torch.zeros(nimg, dtype=torch.float64, device="cuda")
+    nev = torch.zeros(nimg, dtype=torch.int32, device="cuda")
+    outs = capi.Outputs(risk=risk.data_ptr(), risk_evals=nev.data_ptr())
     stream = torch.cuda.current_stream()
 
-    def step():
-        return capi.denoise_device(x.data_ptr(), capi.PGSVT_F32, S, S, nimg, y.data_ptr(),
-                                   est.data_ptr(), p, stream.cuda_stream)
+    def step(prm=p):
+        return capi.denoise_device_ex(x.data_ptr(), capi.PGSVT_F32, S, S, nimg, y.data_ptr(),
+                                      est.data_ptr(), prm, outs, stream.cuda_stream)
 
     for _ in range(args.warmup):
         st = step()
@@ -228,6 +239,45 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * nimg / (ms / 1e3)
+    plain = {"risk": risk.cpu().numpy().copy(), "evals": nev.cpu().numpy().copy(),
+             "lambda": est.cpu().numpy()[:nimg].copy(),
+             "psnr": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
+
+    # ---- learned-lambda form: the shipped MLP's proposal + narrow search
+    learned = None
+    if not args.no_learned:
+        model = pkg.learned.load_model()
+        pl = params(capi, a, m, s, args.patch, -1.0)
+        pl.lambda_model = model.ctypes.data
+        step(pl)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        lst = [step(pl) for _ in range(args.steps)]
+        f1.record(stream)
+        torch.cuda.synchronize()
+        lms = f0.elapsed_time(f1) / args.steps
+        if dist:
+            t = torch.tensor([lms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            lms = float(t.item())
+        lr = risk.cpu().numpy()
+        gap = (lr - plain["risk"]) / np.abs(plain["risk"])
+        lpsnr = psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))
+        learned = {"value": world * nimg / (lms / 1e3), "unit": "frames/s", "ms_per_step": lms,
+                   "speedup_vs_plain": ms / lms,
+                   "risk_evals_per_window": float(nev.cpu().numpy().mean()),
+                   "plain_risk_evals_per_window": float(plain["evals"].mean()),
+                   "risk_gap_max": float(gap.max()), "risk_gap_mean": float(gap.mean()),
+                   "windows_gap_le_1pct": float(np.mean(gap <= 0.01)),
+                   "psnr_db": lpsnr, "plain_psnr_db": plain["psnr"],
+                   "psnr_delta_db": lpsnr - plain["psnr"],
+                   "gpu_launches": int(sum(q.kernel_launches for q in lst)),
+                   "model": "pgure-svt_gb300/lambda_mlp.npz (67-128-128-128-1 GELU, bf16 "
+                            "weights, trained on the GPU by pgsvt_lambda_train)"}
 
     # ---- end to end through pgsvt_denoise with pinned host buffers
     xh = torch.from_numpy(np.ascontiguousarray(noisy.ravel(order="F"))).pin_memory()
@@ -295,7 +345,8 @@ def main():
                                    % (S, S, nimg, args.patch, M, a, m, s),
                        "lambda_search": "plain" if args.hint <= 0 else "hinted %g" % args.hint,
                        "l2": "input larger than L2 (no flush needed)"},
-            "e2e": e2e, "roofline": roof, "clocks": clk,
+            "e2e": e2e, "roofline": roof, "clocks": clk, "learned": learned,
+            "psnr_db_vs_clean": plain["psnr"],
             "gpu_launches": int(sum(x.kernel_launches for x in stats)),
             "stage_seconds_per_step": stage,
             "risk_evals_per_window": evals_per_window,

@@ -100,7 +100,36 @@ typedef struct {
   double hint_span;         /* bracket [hint/span, hint*span] (0: 2.0)  */
   uint32_t frame_begin;     /* output frames [frame_begin, frame_end) are */
   uint32_t frame_end;       /* computed (0,0: all); others are left zero  */
+  /* Learned lambda proposal (not in the reference): a host array of
+   * PGSVT_LAMBDA_MODEL_FLOATS floats (see pgsvt_lambda_train), NULL: off.
+   * Each window's proposal replaces lambda_hint for that window.           */
+  const float* lambda_model;
+  uint32_t hint_points;     /* lambda values per narrow-search round (0: 4) */
+  uint32_t hint_rounds;     /* refinement rounds of the narrow search (0: 1) */
+  double hint_flat;         /* a best point on the narrow grid's edge is kept
+                               when its neighbour's risk is within this
+                               relative amount (0: 1e-3); else the plain
+                               search runs                                   */
+  uint32_t autotune;        /* 1: time the SVD kernel shapes on the first
+                               window batch of each patch size / window
+                               length seen by the process and keep the
+                               fastest (results agree to FP32 rounding);
+                               0: the default shape; 2: the alternative
+                               shape where the patch size has one            */
 } pgsvt_params;
+
+/* Optional per-frame outputs of pgsvt_denoise_ex / pgsvt_denoise_device_ex
+ * (host memory for the former, device memory for the latter; any member may
+ * be NULL).                                                                  */
+typedef struct {
+  float* lambda_features;   /* nframes x PGSVT_LAMBDA_FEATURES, row t at
+                               t*PGSVT_LAMBDA_FEATURES                      */
+  float* lambda_proposals;  /* nframes: model output log10(lambda/upper)
+                               (NaN without a model)                       */
+  double* risk;             /* nframes: PGURE risk at the returned lambda
+                               (0 when not optimising)                     */
+  uint32_t* risk_evals;     /* nframes: lambda values evaluated            */
+} pgsvt_outputs;
 
 /* Per-call report.  All times are wall seconds measured by the library. */
 typedef struct {
@@ -123,6 +152,8 @@ typedef struct {
   uint64_t svd_fp64_tests;  /* Jacobi convergence tests decided in FP64   */
   uint64_t svd_warp_sweeps; /* Jacobi sweeps summed over warps            */
   char message[256];        /* human-readable error / note                */
+  int32_t svd_variant;      /* SVD kernel shape used (0: default)         */
+  int32_t svd_tuned;        /* 1 if this call ran the autotuner           */
 } pgsvt_status;
 
 /* Fill *p with the reference defaults (pguresvt/_pguresvt.pyx:151-168 and
@@ -149,6 +180,100 @@ int pgsvt_denoise_device(const void* X_dev, int32_t dtype, uint32_t nrows,
                          uint32_t ncols, uint32_t nframes, double* Y_dev,
                          double* estimates_dev, const pgsvt_params* p,
                          void* stream, pgsvt_status* st);
+
+/* pgsvt_denoise / pgsvt_denoise_device plus the optional per-frame outputs
+ * listed in a pgsvt_outputs struct; `out` may be NULL.                      */
+int pgsvt_denoise_ex(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                     uint32_t nframes, double* Y, double* estimates,
+                     const pgsvt_params* p, const pgsvt_outputs* out,
+                     pgsvt_status* st);
+int pgsvt_denoise_device_ex(const void* X_dev, int32_t dtype, uint32_t nrows,
+                            uint32_t ncols, uint32_t nframes, double* Y_dev,
+                            double* estimates_dev, const pgsvt_params* p,
+                            const pgsvt_outputs* out_dev, void* stream,
+                            pgsvt_status* st);
+
+/* --- Batches of sequences (config of uneven sizes; not in the reference) ---
+ *
+ * One sequence of a batch.  X, Y and estimates are host memory as in
+ * pgsvt_denoise.  With `lambdas` (nlambdas <= 16 values), every window
+ * evaluates the PGURE risk of exactly those values (one round, together)
+ * and is reconstructed at the one of least risk; `risks` (optional,
+ * nframes x nlambdas, row t at t*nlambdas) receives them.  Without a list
+ * the window runs the lambda search of `params`.  `status` (optional)
+ * receives the sequence's own report.                                       */
+typedef struct {
+  const void* X;
+  int32_t dtype;
+  uint32_t nrows, ncols, nframes;
+  double* Y;
+  double* estimates;
+  const pgsvt_params* params;
+  const double* lambdas;
+  uint32_t nlambdas;
+  double* risks;
+  pgsvt_status* status;
+} pgsvt_sequence;
+
+/* Denoise nseq sequences of any sizes, patch sizes and trajectory lengths on
+ * the current device.  A host work queue hands the sequences, largest first,
+ * to `slots` concurrent workers (0: 2), each with its own stream, so that
+ * one sequence's uploads, ARPS and search overlap another's SVD.  `st`
+ * (optional) receives the totals; the return value is the first failing
+ * sequence's code (PGSVT_OK if none).                                       */
+int pgsvt_denoise_batch(const pgsvt_sequence* seqs, uint32_t nseq, uint32_t slots,
+                        pgsvt_status* st);
+
+/* --- Learned lambda proposal (not in the reference) ---
+ *
+ * A window's features are the three noise parameters as its risk uses them
+ * (after the PGSVT_COMPAT_SWAP_MU_SIGMA binding), each as asinh(1000 v)/8,
+ * and a 64-bin histogram of log10 of the singular values of 4096 of its
+ * kept patches (stratified, seeded choice; all patches when fewer), bins of
+ * width 6/64 over [-4, 2), clamped at both ends, counts divided by the
+ * number of values.  The MLP maps them to y = log10(lambda/upper):
+ *   x0 = (f - mean) * scale
+ *   a1 = gelu(W1 x0 + b1), a2 = gelu(W2 a1 + b2), a3 = gelu(W3 a2 + b3)
+ *   y  = (W4 a3 + b4) * y_scale + y_mean
+ * with gelu(z) = z/2 (1 + erf(z/sqrt 2)).  W1..W4 are used rounded to bf16
+ * (round to nearest even); biases, activations and sums are FP32.
+ * Model array (floats): mean[67] scale[67] W1[128][67] b1[128] W2[128][128]
+ * b2[128] W3[128][128] b3[128] W4[128] b4 y_mean y_scale.  The trainable
+ * parameters are the PGSVT_LAMBDA_PARAMS floats from W1 to b4.            */
+#define PGSVT_LAMBDA_FEATURES 67
+#define PGSVT_LAMBDA_HIDDEN 128
+#define PGSVT_LAMBDA_SAMPLES 4096
+#define PGSVT_LAMBDA_MODEL_FLOATS 41993
+#define PGSVT_LAMBDA_PARAM_OFFSET 134
+#define PGSVT_LAMBDA_PARAMS 41857
+
+/* Model outputs y for n feature rows (host buffers). */
+int pgsvt_lambda_predict(const float* model, const float* features, uint32_t n, float* y);
+
+/* Gradient of the loss L = (1/n) sum_i (o_i - t_i)^2, o_i the network output
+ * before the y_scale/y_mean map and t_i = (target_i - y_mean)/y_scale, with
+ * respect to the PGSVT_LAMBDA_PARAMS trainable floats (taken at their bf16
+ * values for the weights).  Host buffers; *loss receives L.               */
+int pgsvt_lambda_grad(const float* model, const float* features, const float* targets,
+                      uint32_t n, float* grad, double* loss);
+
+typedef struct {
+  uint32_t epochs;          /* passes over the samples                     */
+  uint32_t batch;           /* samples per step (multiple of 32)           */
+  float lr, lr_final;       /* AdamW step size, cosine-decayed to lr_final */
+  float weight_decay;       /* decoupled decay (weights only)              */
+  float beta1, beta2, eps;  /* Adam moments                                */
+  uint64_t seed;            /* shuffling                                   */
+} pgsvt_train_params;
+
+/* Train the model in place on the device (FP32 master weights, bf16 weights
+ * in the forward and backward passes, AdamW), one CUDA graph per epoch.
+ * `model` holds the initial values, including mean/scale/y_mean/y_scale,
+ * which training keeps.  epoch_loss (may be NULL) receives the mean loss of
+ * each epoch.                                                               */
+int pgsvt_lambda_train(float* model, const float* features, const float* targets,
+                       uint32_t n, const pgsvt_train_params* tp, float* epoch_loss,
+                       pgsvt_status* st);
 
 /* --- Component entry points (one reference stage each, host buffers) --- */
 
@@ -188,6 +313,14 @@ int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin,
                       const int32_t* cols, double alpha, double mu,
                       double sigma, int64_t random_seed, uint32_t compat_flags,
                       const double* lambdas, uint32_t nl, double* risk);
+
+/* Median pre-filter of the ARPS input for `nframes` uint16 frames
+ * (ConstantTimeMedianFilter, medfilter.hpp:478-541, as called in
+ * pguresvt.hpp:69-80): the median of the (2r+1)^2 window with coordinates
+ * clamped to the frame.  src and dst are host arrays of nrows x ncols x
+ * nframes (column-major); 1 <= r <= 15 and 2r+1 <= min(nrows, ncols).     */
+int pgsvt_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nrows, uint32_t ncols,
+                        uint32_t nframes, uint32_t r);
 
 /* Singular values of one window without any device allocation.
  *

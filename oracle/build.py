@@ -8,7 +8,10 @@ oracle's ARPS costs and argmins are the same bits on both machines.
 When the reference tree is present (``--ref`` or ``build_ref()``), it also
 builds ``oracle/_ref/ref_probes``: a probe dump program compiled against the
 reference's own vendored PCG header (src/pcg/pcg_random.hpp), used only to
-generate the golden probe fixtures in tests/golden/.
+generate the golden probe fixtures in tests/golden/, and
+``oracle/_ref/libref_medfilter.so``: the reference's constant-time median
+filter (src/medfilter.hpp) compiled from its header, used to generate the
+golden median fixtures and to check the oracle's median restatement.
 """
 import os
 import subprocess
@@ -19,6 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpgsvt_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_PROBES = os.path.join(REF_DIR, "ref_probes")
+REF_MEDIAN = os.path.join(REF_DIR, "libref_medfilter.so")
 REFERENCE_SRC = "/root/reference/src"
 
 
@@ -64,7 +68,24 @@ def build_ref(force=False):
     return REF_PROBES
 
 
+def build_ref_median(force=False):
+    """Compile the reference's median filter (src/medfilter.hpp, plain C)
+    behind oracle/ref_medfilter.c.  Returns the library path, or None when
+    the reference tree is absent."""
+    hdr = os.path.join(REFERENCE_SRC, "medfilter.hpp")
+    if not os.path.exists(hdr):
+        return None
+    src = os.path.join(HERE, "ref_medfilter.c")
+    if not force and not _stale(REF_MEDIAN, [src]):
+        return REF_MEDIAN
+    os.makedirs(REF_DIR, exist_ok=True)
+    subprocess.run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-I", REFERENCE_SRC,
+                    "-o", REF_MEDIAN, src, "-lm"], check=True)
+    return REF_MEDIAN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
     if "--ref" in sys.argv:
         print(build_ref(force=True))
+        print(build_ref_median(force=True))

@@ -7,6 +7,7 @@ pgsvt_oracle.cpp for the line-by-line map.  LAPACK dgesdd comes from scipy's
 ``cython_lapack`` export table, which exists on every machine with scipy.
 """
 import ctypes
+import types
 import os
 import sys
 
@@ -37,7 +38,11 @@ class OrcParams(ctypes.Structure):
         ("search_points", ctypes.c_uint32), ("search_rounds", ctypes.c_uint32),
         ("window_batch", ctypes.c_uint32), ("lambda_hint", ctypes.c_double),
         ("hint_span", ctypes.c_double), ("frame_begin", ctypes.c_uint32),
-        ("frame_end", ctypes.c_uint32),
+        ("frame_end", ctypes.c_uint32), ("lambda_model", ctypes.c_void_p),
+        ("hint_points", ctypes.c_uint32), ("hint_rounds", ctypes.c_uint32),
+        ("hint_flat", ctypes.c_double), ("autotune", ctypes.c_uint32),
+        ("lambda_hints", ctypes.c_void_p),
+        ("risk_out", ctypes.c_void_p), ("evals_out", ctypes.c_void_p),
     ]
 
 
@@ -52,7 +57,8 @@ DEFAULTS = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7,
                 lambda_=-1.0, alpha=-1.0, mu=-1.0, sigma=-1.0, tol=1e-7,
                 compat_flags=COMPAT_ALL, search_points=8, search_rounds=4,
                 window_batch=0, lambda_hint=-1.0, hint_span=2.0, frame_begin=0,
-                frame_end=0)
+                frame_end=0, lambda_model=None, hint_points=4, hint_rounds=1, hint_flat=1e-3,
+                autotune=0, lambda_hints=None, risk_out=None, evals_out=None)
 
 _lib = None
 
@@ -90,6 +96,7 @@ def lib():
             ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
             ctypes.c_double, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
             ctypes.c_void_p]
+        L.orc_median_filter.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3
         L.orc_denoise.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [
             P(OrcParams), ctypes.c_void_p, ctypes.c_void_p, P(OrcReport)]
         L.orc_time_sample.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
@@ -194,17 +201,39 @@ def risk_window(u, bs, ov, rows, cols, lambdas, alpha, mu, sigma, seed, compat=C
     return out
 
 
-def denoise(X, **kw):
-    """Whole-sequence denoise; X is (rows, cols, frames).  Returns (Y, est, report)."""
+def median_filter(frame, r):
+    """Median pre-filter of one uint16 frame (rows, cols), column-major as the
+    reference's slices."""
+    a = np.asfortranarray(frame, dtype=np.uint16)
+    out = np.zeros_like(a, order="F")
+    _check(lib().orc_median_filter(_ptr(a), _ptr(out), a.shape[0], a.shape[1], r))
+    return out
+
+
+def denoise(X, lambda_hints=None, **kw):
+    """Whole-sequence denoise; X is (rows, cols, frames).  Returns (Y, est, report);
+    the report also carries per-frame `risk` and `evals`.  `lambda_hints` (one
+    value per frame) centres each window's narrow search."""
     X = _cube(X)
     nr, nc, nt = X.shape
+    risk = np.zeros(nt, np.float64)
+    evals = np.zeros(nt, np.uint32)
+    hints = None
+    if lambda_hints is not None:
+        hints = np.ascontiguousarray(lambda_hints, np.float64)
+        assert hints.shape == (nt,)
+        kw["lambda_hints"] = hints.ctypes.data
+    kw["risk_out"] = risk.ctypes.data
+    kw["evals_out"] = evals.ctypes.data
     p = make_params(**kw)
     Y = np.zeros((nr, nc, nt), np.float64, order="F")
     est = np.zeros((nt, 4), np.float64, order="F")
     rep = OrcReport()
     _check(lib().orc_denoise(_ptr(X), nr, nc, nt, ctypes.byref(p), _ptr(Y), _ptr(est),
                              ctypes.byref(rep)))
-    return Y, est, rep
+    out = types.SimpleNamespace(windows=rep.windows, risk_evals=rep.risk_evals,
+                                seconds=rep.seconds, risk=risk, evals=evals)
+    return Y, est, out
 
 
 def time_sample(X, first, nwindows, threads, stride, evals, **kw):

@@ -546,12 +546,18 @@ struct Pgure {
 struct SearchResult {
   double lambda, risk;
   uint32_t evals;
-  bool edge;  // best point at an end of the round-0 grid
+  bool edge;  // stopped after the round-0 grid: best point on a steep edge
 };
 
+// edge_flat >= 0: after the round-0 grid, a best point at either end whose
+// neighbour's risk exceeds it by more than edge_flat * |risk| ends the search
+// with edge = true (the narrow search's hand-over to the plain one), unless
+// that end is a bound of the search: the bottom when include_zero_lo, the
+// top when it equals `upper`.
 template <typename F>
 SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t rounds,
-                          double tol, uint32_t max_eval, bool include_zero_lo) {
+                          double tol, uint32_t max_eval, bool include_zero_lo,
+                          double edge_flat = -1.0, double upper = -1.0) {
   struct Pt { double l, r; };
   std::vector<Pt> pts;
   if (max_eval < K) K = std::max<uint32_t>(1, max_eval);
@@ -567,7 +573,16 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
     return b;
   };
   size_t b = best_of();
-  SearchResult res{pts[b].l, pts[b].r, evals, b == 0 || b + 1 == pts.size()};
+  SearchResult res{pts[b].l, pts[b].r, evals, false};
+  const bool bound = (b == 0 && include_zero_lo) || (b + 1 == pts.size() && pts[b].l >= upper &&
+                                                     upper > 0.0);
+  if (edge_flat >= 0.0 && (b == 0 || b + 1 == pts.size()) && !bound) {
+    const size_t nb = (b == 0) ? 1 : pts.size() - 2;
+    if (pts.size() < 2 || !(pts[nb].r - pts[b].r <= edge_flat * std::fabs(pts[b].r))) {
+      res.edge = true;
+      return res;
+    }
+  }
   for (uint32_t rd = 0; rd < rounds && evals + K <= max_eval; ++rd) {
     const double blo = (b > 0) ? pts[b - 1].l : (include_zero_lo ? 0.0 : pts[b].l);
     const double bhi = (b + 1 < pts.size()) ? pts[b + 1].l : pts[b].l;
@@ -586,6 +601,40 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
   }
   res.evals = evals;
   return res;
+}
+
+// ---- median pre-filter of the ARPS input (pguresvt.hpp:69-84)
+//
+// X is converted to uint16 slice by slice (arma::conv_to<Mat<uint16_t>>;
+// Armadillo 9.880.1 is not in the reference tree: this restatement takes C's
+// conversion, truncation toward zero, with values clamped to [0, 65535]) and
+// filtered by ConstantTimeMedianFilter (medfilter.hpp:478-541) with radius
+// medianSize.  That filter (one stripe here: its stripe count works out to 1
+// for every radius, the unsigned arithmetic of medfilter.hpp:512-513) is the
+// exact median of the (2r+1)^2 window with coordinates clamped to the frame
+// (replicated borders: medfilter.hpp:365-377 for rows, the pad_left /
+// pad_right paths for columns).  Restated here as a direct selection.
+uint16_t to_u16(double x) {
+  if (!(x > 0.0)) return 0;
+  if (x >= 65535.0) return 65535;
+  return (uint16_t)x;
+}
+
+void median_frame(const uint16_t* src, uint16_t* dst, int nx, int ny, int r) {
+  std::vector<uint16_t> win((size_t)(2 * r + 1) * (2 * r + 1));
+  for (int i = 0; i < ny; ++i)
+    for (int j = 0; j < nx; ++j) {
+      size_t k = 0;
+      for (int di = -r; di <= r; ++di) {
+        const int ii = std::min(std::max(i + di, 0), ny - 1);
+        for (int dj = -r; dj <= r; ++dj) {
+          const int jj = std::min(std::max(j + dj, 0), nx - 1);
+          win[k++] = src[(size_t)ii * nx + jj];
+        }
+      }
+      std::nth_element(win.begin(), win.begin() + k / 2, win.begin() + k);
+      dst[(size_t)i * nx + j] = win[k / 2];
+    }
 }
 
 struct Plan {
@@ -618,7 +667,8 @@ void validate(const orc_params& p, uint32_t nrows, uint32_t ncols, uint32_t nimg
   Plan pl(p, nrows, nimg);
   if (pl.Ntc < 1 || nimg < pl.nwin) throw Fail(1, "sequence shorter than the trajectory window");
   if (p.motion_estimation && p.motion_window < 1) throw Fail(1, "motion_window must be >= 1");
-  if (p.median_size > 0) throw Fail(2, "median pre-filter not restated in the oracle");
+  if (p.median_size > 0 && 2 * p.median_size + 1 > nrows)
+    throw Fail(1, "median window wider than the frame (medfilter.hpp:347-348)");
   if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0))
     throw Fail(2, "noise estimation not restated in the oracle: give alpha, mu, sigma");
   if (!p.optimize_pgure && p.lambda < 0) throw Fail(1, "lambda must be >= 0 without optimisation");
@@ -630,18 +680,26 @@ struct WindowOut {
   uint32_t evals;
 };
 
-WindowOut run_window(const double* X, const orc_params& p, const Plan& pl, uint32_t t,
-                     double* Yslice) {
+WindowOut run_window(const double* X, const double* Z, const orc_params& p, const Plan& pl,
+                     uint32_t t, double* Yslice) {
   const Geom g(pl.nrows, pl.bs, pl.nwin);
   const size_t F = g.frame(), C = g.cube();
   std::vector<double> u(X + (size_t)pl.start(t) * F, X + (size_t)pl.start(t) * F + C);
   double umax = u[0];
   for (double x : u) umax = std::max(umax, x);
   for (double& x : u) x /= umax;
-  // w == u: no median filter (medianSize <= 0), pguresvt.hpp:85-88,116-120
+  // ARPS input w: the median-filtered window over its own maximum, or u
+  // itself without the filter (pguresvt.hpp:85-88,100-120)
+  std::vector<double> w;
+  if (Z) {
+    w.assign(Z + (size_t)pl.start(t) * F, Z + (size_t)pl.start(t) * F + C);
+    double wmax = w[0];
+    for (double x : w) wmax = std::max(wmax, x);
+    for (double& x : w) x /= wmax;
+  }
   std::vector<int32_t> rows((size_t)g.P * g.nwin), cols((size_t)g.P * g.nwin);
   {
-    Arps a(u.data(), g, pl.mw, rows.data(), cols.data());
+    Arps a(Z ? w.data() : u.data(), g, pl.mw, rows.data(), cols.data());
     a.estimate(t, pl.fw, pl.nimg, p.motion_estimation != 0, p.compat_flags & kCompatZeroMotion);
   }
   Pgure pg(g, u.data(), patch_list(g.S, g.bs, pl.ov), rows.data(), cols.data(), p.alpha,
@@ -658,10 +716,16 @@ WindowOut run_window(const double* X, const orc_params& p, const Plan& pl, uint3
     const uint32_t maxe = p.max_iter ? p.max_iter : 1;
     auto rf = [&](double l) { return pg.risk(l); };
     SearchResult sr;
-    if (p.lambda_hint > 0) {
+    const double hint = p.lambda_hints ? p.lambda_hints[t] : p.lambda_hint;
+    if (hint > 0) {
       const double span = p.hint_span > 1 ? p.hint_span : 2.0;
-      sr = batch_search(rf, p.lambda_hint / span, std::min(upper, p.lambda_hint * span), K,
-                        std::max<uint32_t>(1, R / 2), p.tol, maxe, false);
+      const uint32_t Kh = std::min(K, p.hint_points ? p.hint_points : 4u);
+      const uint32_t Rh = p.hint_rounds ? p.hint_rounds : 1u;
+      const double flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
+      const double h = std::min(hint, upper);
+      const double lo = h / span;
+      sr = batch_search(rf, lo, std::min(upper, h * span), Kh, Rh, p.tol, maxe,
+                        lo <= upper * 1e-4, flat, upper);
       if (sr.edge) {  // proposal not bracketed: fall back to the full search
         const SearchResult full = batch_search(rf, upper * 1e-4, upper, K, R, p.tol,
                                                maxe > sr.evals ? maxe - sr.evals : 1, true);
@@ -788,6 +852,11 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs, 
   });
 }
 
+int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,
+                      uint32_t r) {
+  return guarded([&] { median_frame(src, dst, (int)nx, (int)ny, (int)r); });
+}
+
 int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimages,
                 const orc_params* p, double* Y, double* est, orc_report* rep) {
   return guarded([&] {
@@ -801,14 +870,27 @@ int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimage
     uint32_t fb = p->frame_begin, fe = p->frame_end;  // output frames computed
     if (fb == 0 && fe == 0) fe = nimages;
     if (fb >= fe || fe > nimages) throw Fail(1, "bad frame range");
+    std::vector<double> Z;
+    if (p->median_size > 0) {  // pguresvt.hpp:69-80
+      Z.resize(F * nimages);
+      fan_out(nimages, p->n_jobs, [&](uint32_t i) {
+        std::vector<uint16_t> a(F), b(F);
+        for (size_t k = 0; k < F; ++k) a[k] = to_u16(X[(size_t)i * F + k]);
+        median_frame(a.data(), b.data(), (int)ncols, (int)nrows, (int)p->median_size);
+        for (size_t k = 0; k < F; ++k) Z[(size_t)i * F + k] = b[k];
+      });
+    }
     fan_out(fe - fb, p->n_jobs, [&](uint32_t k) {
       const uint32_t t = fb + k;
-      const WindowOut o = run_window(X, *p, pl, t, Y + (size_t)t * F);
+      const WindowOut o = run_window(X, Z.empty() ? nullptr : Z.data(), *p, pl, t,
+                                     Y + (size_t)t * F);
       est[t] = o.lambda;  // pguresvt.hpp:150-153 (unswapped alpha, mu, sigma)
       est[t + nimages] = p->alpha;
       est[t + 2 * (size_t)nimages] = p->mu;
       est[t + 3 * (size_t)nimages] = p->sigma;
       evals[t] = o.evals;
+      if (p->risk_out) p->risk_out[t] = o.risk;
+      if (p->evals_out) p->evals_out[t] = o.evals;
     });
     if (rep) {
       rep->windows = fe - fb;

@@ -33,6 +33,15 @@ typedef struct {
   uint32_t compat_flags, search_points, search_rounds, window_batch;
   double lambda_hint, hint_span;
   uint32_t frame_begin, frame_end;
+  const float* lambda_model;  /* unused by the oracle (layout only) */
+  uint32_t hint_points, hint_rounds;
+  double hint_flat;
+  uint32_t autotune;  /* unused by the oracle (layout only) */
+  /* oracle only: per-frame narrow-search centres (NULL: lambda_hint for all)
+   * and per-frame outputs (NULL: not written) */
+  const double* lambda_hints;
+  double* risk_out;
+  uint32_t* evals_out;
 } orc_params;
 
 typedef struct {
@@ -70,6 +79,11 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs,
                     const int32_t* cols, double alpha, double mu, double sigma,
                     int64_t seed, uint32_t compat, const double* lambdas,
                     uint32_t nl, double* risk);
+
+/* Median of the (2r+1)^2 window with clamped coordinates (the reference's
+ * ConstantTimeMedianFilter, medfilter.hpp:478-541); nx is the fast axis. */
+int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,
+                      uint32_t r);
 
 /* Whole sequence (PGURESVT<T1,double>, pguresvt.hpp:17-172); X is FP64. */
 int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols,

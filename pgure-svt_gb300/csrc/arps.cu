@@ -223,19 +223,25 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
   if (cn.npairs == 0) return;
   const WinConst& wc = d.wc[w];
   const size_t F = g.F();
+  // ARPS input: the median-filtered window when the pre-filter is on
+  // (its values are integers, exact in FP32), else the window itself
+  const bool med = d.zs != nullptr;
+  const float* fw = med ? d.wz : d.u;
+  const float* xw = med ? d.zs : d.xs;
+  const double* xd = med ? nullptr : d.x64;
   ArpsCtx c;
-  c.umax = wc.unorm;
+  c.umax = med ? wc.wnorm : wc.unorm;
   c.S = g.S;
   c.mw = g.mw;
   int my = 0, mx = 0;
   for (int q = 0; q < cn.npairs; ++q) {
     const int a1 = cn.a1[q], a2 = cn.a2[q];
-    c.fa1 = d.u + ((size_t)w * g.nwin + a1) * F;
-    c.fa2 = d.u + ((size_t)w * g.nwin + a2) * F;
-    c.xa1 = d.xs + (size_t)(wc.s0 + a1) * F;
-    c.xa2 = d.xs + (size_t)(wc.s0 + a2) * F;
-    c.xa1d = d.x64 ? d.x64 + (size_t)(wc.s0 + a1) * F : nullptr;
-    c.xa2d = d.x64 ? d.x64 + (size_t)(wc.s0 + a2) * F : nullptr;
+    c.fa1 = fw + ((size_t)w * g.nwin + a1) * F;
+    c.fa2 = fw + ((size_t)w * g.nwin + a2) * F;
+    c.xa1 = xw + (size_t)(wc.s0 + a1) * F;
+    c.xa2 = xw + (size_t)(wc.s0 + a2) * F;
+    c.xa1d = xd ? xd + (size_t)(wc.s0 + a1) * F : nullptr;
+    c.xa2d = xd ? xd + (size_t)(wc.s0 + a2) * F : nullptr;
     int oy, ox;
     arps_pair<BS>(c, it, my, mx, oy, ox, d.counters);
     d.pos[((size_t)w * g.nwin + a2) * g.P + it] = (uint32_t)oy | ((uint32_t)ox << 16);

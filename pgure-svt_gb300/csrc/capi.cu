@@ -11,7 +11,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <thread>
+#include <atomic>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -127,6 +131,35 @@ std::vector<int32_t> tile_order(const std::vector<int32_t>& plist, int S, int bs
   return out;
 }
 
+// Kept patches whose singular values make up a window's lambda features: a
+// stratified choice of PGSVT_LAMBDA_SAMPLES of them (all of them when fewer)
+// in the reference's sorted order, sample i drawn from stratum i at an
+// offset given by the lowbias32 integer hash (C. Wellons) of i.  Returned as
+// processing slots.
+uint32_t lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+std::vector<int32_t> feature_slots(const std::vector<int32_t>& sorted,
+                                   const std::vector<int32_t>& plist, int P) {
+  const uint64_t NP = sorted.size();
+  const uint64_t ns = std::min<uint64_t>(NP, PGSVT_LAMBDA_SAMPLES);
+  std::vector<int32_t> slot_of(P, -1);
+  for (size_t k = 0; k < plist.size(); ++k) slot_of[plist[k]] = (int32_t)k;
+  std::vector<int32_t> out(ns);
+  for (uint64_t i = 0; i < ns; ++i) {
+    const uint64_t h = lowbias32((uint32_t)i ^ 0x5eed1234u);
+    const uint64_t k = (i * NP + ((h * NP) >> 32)) / ns;
+    out[i] = slot_of[sorted[k]];
+  }
+  return out;
+}
+
 // Frame pairs of MotionEstimator::Estimate (arps.hpp:52-134) grouped into
 // chains of pairs that share a motion slot (the only data dependence).
 std::vector<ArpsChain> chains_for(int t, int tw, int nimg, int nwin) {
@@ -181,6 +214,7 @@ struct DevMem {
 struct Stats {
   uint64_t launches = 0, h2d = 0, d2h = 0, evals = 0, windows = 0;
   uint64_t svd_launches = 0, svd_matrices = 0, arps_exact = 0, svd_fp64 = 0, svd_sweeps = 0;
+  int svd_variant = 0, svd_tuned = 0;
   double stage[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
@@ -238,8 +272,10 @@ void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
     throw Fail(PGSVT_ERR_UNSUPPORTED, "trajectory window above 21 frames in this build");
   if (p.motion_estimation && (p.motion_window < 2 || p.motion_window > (uint32_t)kMaxMW))
     throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid motion_window parameter: must be in [2, 15]");
-  if (p.median_size > 0)
-    throw Fail(PGSVT_ERR_UNSUPPORTED, "median pre-filter (motion_filter) is not built; pass <= 0");
+  if (p.median_size > kMaxMedian)
+    throw Fail(PGSVT_ERR_UNSUPPORTED, "motion_filter (median radius) above 15 in this build");
+  if (p.median_size > 0 && 2 * p.median_size + 1 > (int64_t)nr)
+    throw Fail(PGSVT_ERR_INVALID_ARG, "motion_filter window wider than the frame");
   if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0))
     throw Fail(PGSVT_ERR_UNSUPPORTED,
                "noise estimation is not built: give noise alpha, mu and sigma (>= 0)");
@@ -256,7 +292,7 @@ struct Setup {
   std::vector<int32_t> plist;   // processing order
 };
 
-Setup make_setup(const pgsvt_params& p, int S, int nimg) {
+Setup make_setup(const pgsvt_params& p, int S, int nimg, int nfixed = 0) {
   Setup s;
   Geometry& g = s.g;
   g.S = S;
@@ -277,8 +313,16 @@ Setup make_setup(const pgsvt_params& p, int S, int nimg) {
   // bound the points a window keeps
   while (s.K * (1 + s.rounds) > kMaxPts && s.rounds > 0) --s.rounds;
   // plain: 1 grid + rounds refinements; hinted: 1 + rounds/2, then possibly plain again
-  s.max_rounds = p.lambda_hint > 0 ? (1 + std::max(1, s.rounds / 2)) + (1 + s.rounds)
-                                   : 1 + s.rounds;
+  // plain: 1 grid + rounds refinements; narrow (hinted or learned): 1 grid +
+  // hint_rounds refinements, then possibly the plain search
+  const int hr = p.hint_rounds ? (int)p.hint_rounds : 1;
+  const bool narrow = p.lambda_hint > 0 || (p.lambda_model && p.optimize_pgure);
+  s.max_rounds = narrow ? (1 + hr) + (1 + s.rounds) : 1 + s.rounds;
+  if (nfixed > 0) {  // one round over a given lambda list
+    s.K = nfixed;
+    s.rounds = 0;
+    s.max_rounds = 1;
+  }
   return s;
 }
 
@@ -300,7 +344,14 @@ Problem make_problem(const pgsvt_params& p, const Setup& su) {
   pb.rounds = su.rounds;
   pb.hint = p.lambda_hint;
   pb.hint_span = p.hint_span > 1.0 ? p.hint_span : 2.0;
+  pb.hint_K = std::min(su.K, p.hint_points ? (int)p.hint_points : 4);
+  pb.hint_rounds = p.hint_rounds ? (int)p.hint_rounds : 1;
+  pb.hint_flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
   pb.acc64 = 0;
+  pb.svd_variant = 0;
+  pb.fixed = nullptr;
+  pb.nfixed = 0;
+  pb.fixed_risk = nullptr;
   return pb;
 }
 
@@ -310,6 +361,7 @@ size_t window_bytes(const Problem& pb) {
   const size_t C = g.cube(), NP = g.NP, NC = g.NC;
   size_t b = 0;
   b += C * 4;                       // u
+  b += C * 4;                       // wz (median pre-filter; counted always)
   b += (size_t)g.nwin * g.P * 4;    // pos
   b += C * 4;                       // cnt
   b += C * 4 * 3;                   // fields
@@ -336,10 +388,70 @@ struct Lane {
 // The per-sequence engine.  X_dev holds the input (dtype) on the device.
 // Windows are processed in batches of W; batches go round-robin to NS
 // streams, so one batch's lambda search overlaps another batch's SVD.
+// SVD kernel shape chosen by the autotuner per (patch rows, padded columns),
+// process-wide.
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tuned;
+
+// Time every SVD kernel shape of this geometry on the batch at hand (second
+// of two runs each) and keep the fastest; leaves the outputs of the chosen
+// shape in place.
+int tune_svd(Problem& pb, const DeviceBuffers& d, cudaStream_t s, Stats& stats) {
+  const int nv = svd_variants(pb.g.M);
+  cudaEvent_t e0, e1;
+  PGSVT_CK(cudaEventCreate(&e0));
+  PGSVT_CK(cudaEventCreate(&e1));
+  struct EG { cudaEvent_t a, b; ~EG() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
+  int best = 0, last = 0;
+  float best_ms = 0.f;
+  for (int v = 0; v < nv; ++v) {
+    pb.svd_variant = v;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      PGSVT_CK(cudaEventRecord(e0, s));
+      check_launch(launch_svd(pb, d, s), stats);
+      PGSVT_CK(cudaEventRecord(e1, s));
+      PGSVT_CK(cudaEventSynchronize(e1));
+      PGSVT_CK(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    last = v;
+    if (v == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  pb.svd_variant = best;
+  if (best != last) check_launch(launch_svd(pb, d, s), stats);
+  return best;
+}
+
 void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, double* est_dev,
-                  const pgsvt_params& p, cudaStream_t s, Stats& stats) {
-  Setup su = make_setup(p, S, nimg);
+                  const pgsvt_params& p, const pgsvt_outputs* out, cudaStream_t s, Stats& stats,
+                  const double* fixed = nullptr, int nfixed = 0, double* fixed_risk = nullptr) {
+  Setup su = make_setup(p, S, nimg, nfixed);
   Problem pb = make_problem(p, su);
+  DevMem mem0;
+  if (nfixed > 0) {
+    double* f = mem0.arr<double>(nfixed);
+    PGSVT_CK(cudaMemcpyAsync(f, fixed, sizeof(double) * nfixed, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    stats.h2d += sizeof(double) * nfixed;
+    pb.fixed = f;
+    pb.nfixed = nfixed;
+    pb.fixed_risk = fixed_risk;
+  }
+  // SVD kernel shape: tuned once per process and geometry when asked
+  const std::pair<int, int> tkey(pb.g.M, pb.g.NC);
+  bool tune = false;
+  if (p.autotune == 2) {
+    pb.svd_variant = svd_variants(pb.g.M) > 1 ? 1 : 0;
+  } else if (p.autotune) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(tkey);
+    if (it != g_tuned.end()) pb.svd_variant = it->second;
+    else tune = svd_variants(pb.g.M) > 1;
+  }
+  stats.svd_variant = pb.svd_variant;
   const Geometry& g = pb.g;
   DevMem mem;
   const size_t F = g.F(), C = g.cube();
@@ -358,6 +470,15 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   stats.d2h += sizeof(double) * nimg;
   for (double v : hmax)
     if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
+  // median pre-filter of the ARPS input (pguresvt.hpp:69-84)
+  float* zs = nullptr;
+  double* zmx = nullptr;
+  if (p.median_size > 0) {
+    zs = mem.arr<float>((size_t)nimg * F);
+    zmx = mem.arr<double>(nimg);
+    check_launch(launch_median(xs, x64, nimg, S, (int)p.median_size, zs, s), stats);
+    check_launch(launch_frame_max(zs, nullptr, nimg, F, zmx, s), stats);
+  }
 
   const int ncopies = !pb.optimize ? 1 : ((pb.compat & PGSVT_COMPAT_INT_DELTA1) ? 3 : 4);
   // zero-motion quirk: every patch lands on the (0,0) block of the other
@@ -413,6 +534,32 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     PGSVT_CK(cudaMemsetAsync(Y_dev, 0, sizeof(double) * (size_t)nimg * F, s));
     PGSVT_CK(cudaMemsetAsync(est_dev, 0, sizeof(double) * (size_t)nimg * 4, s));
   }
+  // learned lambda proposal: model, its bf16 shadow, the sampled patch slots
+  const bool use_model = pb.optimize && p.lambda_model && pb.nfixed == 0;
+  const bool want_feat = use_model || (out && out->lambda_features);
+  float* dmodel = nullptr;
+  void* dmodel_bf = nullptr;
+  int32_t* fslots = nullptr;
+  int nfslots = 0;
+  if (use_model) {
+    dmodel = mem.arr<float>(PGSVT_LAMBDA_MODEL_FLOATS);
+    dmodel_bf = mem.get(PGSVT_LAMBDA_MODEL_FLOATS * 2);
+    PGSVT_CK(cudaMemcpyAsync(dmodel, p.lambda_model, sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS,
+                             cudaMemcpyHostToDevice, s));
+    stats.h2d += sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS;
+    check_launch(lambda_shadow(dmodel, dmodel_bf, s), stats);
+    PGSVT_CK(lambda_attrs());
+  }
+  if (want_feat) {
+    const std::vector<int32_t> fs = feature_slots(su.sorted, su.plist, g.P);
+    nfslots = (int)fs.size();
+    fslots = mem.arr<int32_t>(fs.size());
+    PGSVT_CK(cudaMemcpyAsync(fslots, fs.data(), sizeof(int32_t) * fs.size(), cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaStreamSynchronize(s));  // fs goes out of scope
+    stats.h2d += sizeof(int32_t) * fs.size();
+  }
+  if (out && out->lambda_proposals && !use_model)  // all-ones bytes: NaN
+    PGSVT_CK(cudaMemsetAsync(out->lambda_proposals, 0xff, sizeof(float) * nimg, s));
   cudaEvent_t ready;
   PGSVT_CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
   struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } evg{ready};
@@ -442,6 +589,9 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.xs = xs;
     d.x64 = x64;
     d.fmax = fmx;
+    d.zs = zs;
+    d.zmax = zmx;
+    if (zs) d.wz = mem.arr<float>((size_t)W * C);
     d.plist = plist;
     d.counters = counters;
     d.Y = Y_dev;
@@ -473,6 +623,20 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
     d.wc = mem.arr<WinConst>(W);
     d.st = mem.arr<SearchState>(W);
+    d.model = dmodel;
+    d.model_bf16 = dmodel_bf;
+    d.feat_slots = fslots;
+    d.nfeat_slots = nfslots;
+    if (want_feat) {
+      d.feat = mem.arr<float>((size_t)W * PGSVT_LAMBDA_FEATURES);
+      d.prop = mem.arr<float>(W);
+    }
+    if (out) {
+      d.feat_out = out->lambda_features;
+      d.prop_out = use_model ? out->lambda_proposals : nullptr;
+      d.risk_out = out->risk;
+      d.evals_out = out->risk_evals;
+    }
     if (pb.optimize) {
       if (shared_probes) {
         d.d1 = sp1;
@@ -515,11 +679,32 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     check_launch(launch_fields(pbb, d, L.s), stats, 4);
     check_launch(launch_search_init(pbb, d, L.s), stats);  // sets the lambda range
     clk.mark(3);
-    check_launch(launch_svd(pbb, d, L.s), stats);
+    if (tune) {
+      const int v = tune_svd(pbb, d, L.s, stats);
+      pb.svd_variant = v;
+      stats.svd_variant = v;
+      stats.svd_tuned = 1;
+      tune = false;
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tuned[tkey] = v;
+    } else {
+      check_launch(launch_svd(pbb, d, L.s), stats);
+    }
     clk.mark(4);
     stats.svd_launches += 1;
     stats.svd_matrices += (uint64_t)pbb.W * ncopies * g.NP;
     stats.windows += pbb.W;
+    if (want_feat) {
+      check_launch(launch_lambda_features(pbb, d, L.s), stats);
+      if (d.feat_out)
+        PGSVT_CK(cudaMemcpyAsync(d.feat_out + (size_t)win0 * PGSVT_LAMBDA_FEATURES, d.feat,
+                                 sizeof(float) * PGSVT_LAMBDA_FEATURES * pbb.W,
+                                 cudaMemcpyDeviceToDevice, L.s));
+    }
+    if (use_model) {
+      check_launch(launch_lambda_propose(pbb, d, L.s), stats);
+      check_launch(launch_search_hint(pbb, d, L.s), stats);
+    }
     if (pbb.optimize)
       for (int r = 0; r < su.max_rounds; ++r) check_launch(launch_eval_round(pbb, d, 0, L.s), stats, 3);
     clk.mark(5);
@@ -581,6 +766,8 @@ int guarded(pgsvt_status* st, Fn&& fn) {
     st->arps_exact_steps = stats.arps_exact;
     st->svd_fp64_tests = stats.svd_fp64;
     st->svd_warp_sweeps = stats.svd_sweeps;
+    st->svd_variant = stats.svd_variant;
+    st->svd_tuned = stats.svd_tuned;
     st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::snprintf(st->message, sizeof(st->message), "%s", g_err.c_str());
   }
@@ -602,6 +789,65 @@ void need_device() {
   const cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0)
     throw Fail(PGSVT_ERR_CUDA, "no CUDA device available (this library has no CPU path)", (int)e);
+}
+
+// Host-memory denoise of one sequence on its own stream (pgsvt_denoise_ex and
+// the batch workers).  `fixed`/`nfixed`: a lambda list evaluated instead of
+// the search, `risks` its per-frame risks (host, nframes x nfixed).
+void denoise_host(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols, uint32_t nframes,
+                  double* Y, double* estimates, const pgsvt_params& p, const pgsvt_outputs* out,
+                  const double* fixed, int nfixed, double* risks, Stats& stats) {
+  const size_t es = dtype_size(dtype);
+  validate(p, nrows, ncols, nframes);
+  if (nfixed > 0 && !p.optimize_pgure)
+    throw Fail(PGSVT_ERR_INVALID_ARG, "a lambda list needs optimize_pgure (its risks are PGURE)");
+  if (nfixed > kMaxK) throw Fail(PGSVT_ERR_INVALID_ARG, "more than 16 lambda values");
+  const size_t n = (size_t)nrows * ncols * nframes;
+  DevMem mem;
+  cudaStream_t s;
+  PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+  void* Xd = mem.get(n * es);
+  double* Yd = mem.arr<double>(n);
+  double* Ed = mem.arr<double>((size_t)nframes * 4);
+  pgsvt_outputs od{};  // device twins of the requested per-frame outputs
+  const size_t nf = nframes, nfe = nf * PGSVT_LAMBDA_FEATURES;
+  if (out) {
+    if (out->lambda_features) od.lambda_features = mem.arr<float>(nfe);
+    if (out->lambda_proposals) od.lambda_proposals = mem.arr<float>(nf);
+    if (out->risk) od.risk = mem.arr<double>(nf);
+    if (out->risk_evals) od.risk_evals = mem.arr<uint32_t>(nf);
+    if (od.lambda_features) PGSVT_CK(cudaMemsetAsync(od.lambda_features, 0, nfe * 4, s));
+    if (od.risk) PGSVT_CK(cudaMemsetAsync(od.risk, 0, nf * 8, s));
+    if (od.risk_evals) PGSVT_CK(cudaMemsetAsync(od.risk_evals, 0, nf * 4, s));
+    if (od.lambda_proposals) PGSVT_CK(cudaMemsetAsync(od.lambda_proposals, 0xff, nf * 4, s));
+  }
+  double* rd = nullptr;
+  if (risks && nfixed > 0) {
+    rd = mem.arr<double>(nf * nfixed);
+    PGSVT_CK(cudaMemsetAsync(rd, 0, nf * nfixed * 8, s));
+  }
+  PGSVT_CK(cudaMemcpyAsync(Xd, X, n * es, cudaMemcpyHostToDevice, s));
+  stats.h2d += n * es;
+  run_sequence(Xd, dtype, (int)nrows, (int)nframes, Yd, Ed, p, out ? &od : nullptr, s, stats,
+               fixed, nfixed, rd);
+  PGSVT_CK(cudaMemcpyAsync(Y, Yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  PGSVT_CK(cudaMemcpyAsync(estimates, Ed, (size_t)nframes * 4 * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  stats.d2h += n * sizeof(double) + (size_t)nframes * 4 * sizeof(double);
+  auto back = [&](void* h, const void* d, size_t b) {
+    if (!h) return;
+    PGSVT_CK(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, s));
+    stats.d2h += b;
+  };
+  if (out) {
+    back(out->lambda_features, od.lambda_features, nfe * 4);
+    back(out->lambda_proposals, od.lambda_proposals, nf * 4);
+    back(out->risk, od.risk, nf * 8);
+    back(out->risk_evals, od.risk_evals, nf * 4);
+  }
+  if (rd) back(risks, rd, nf * nfixed * 8);
+  PGSVT_CK(cudaStreamSynchronize(s));
 }
 
 // ---------------------------------------------------------------------------
@@ -748,45 +994,308 @@ int pgsvt_default_params(pgsvt_params* p) {
   p->hint_span = 2.0;
   p->frame_begin = 0;
   p->frame_end = 0;
+  p->lambda_model = nullptr;
+  p->hint_points = 4;
+  p->hint_rounds = 1;
+  p->hint_flat = 1e-3;
+  p->autotune = 0;
   return PGSVT_OK;
 }
 
-int pgsvt_denoise_device(const void* X_dev, int32_t dtype, uint32_t nrows, uint32_t ncols,
-                         uint32_t nframes, double* Y_dev, double* est_dev, const pgsvt_params* p,
-                         void* stream, pgsvt_status* st) {
+int pgsvt_denoise_device_ex(const void* X_dev, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                            uint32_t nframes, double* Y_dev, double* est_dev,
+                            const pgsvt_params* p, const pgsvt_outputs* out_dev, void* stream,
+                            pgsvt_status* st) {
   return guarded(st, [&](Stats& stats) {
     if (!X_dev || !Y_dev || !est_dev || !p) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
     need_device();
     dtype_size(dtype);
     validate(*p, nrows, ncols, nframes);
     cudaStream_t s = (cudaStream_t)stream;
-    run_sequence(X_dev, dtype, (int)nrows, (int)nframes, Y_dev, est_dev, *p, s, stats);
+    run_sequence(X_dev, dtype, (int)nrows, (int)nframes, Y_dev, est_dev, *p, out_dev, s, stats);
+  });
+}
+
+int pgsvt_denoise_device(const void* X_dev, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                         uint32_t nframes, double* Y_dev, double* est_dev, const pgsvt_params* p,
+                         void* stream, pgsvt_status* st) {
+  return pgsvt_denoise_device_ex(X_dev, dtype, nrows, ncols, nframes, Y_dev, est_dev, p, nullptr,
+                                 stream, st);
+}
+
+int pgsvt_denoise_ex(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols,
+                     uint32_t nframes, double* Y, double* estimates, const pgsvt_params* p,
+                     const pgsvt_outputs* out, pgsvt_status* st) {
+  return guarded(st, [&](Stats& stats) {
+    if (!X || !Y || !estimates || !p) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    need_device();
+    denoise_host(X, dtype, nrows, ncols, nframes, Y, estimates, *p, out, nullptr, 0, nullptr,
+                 stats);
   });
 }
 
 int pgsvt_denoise(const void* X, int32_t dtype, uint32_t nrows, uint32_t ncols, uint32_t nframes,
                   double* Y, double* estimates, const pgsvt_params* p, pgsvt_status* st) {
-  return guarded(st, [&](Stats& stats) {
-    if (!X || !Y || !estimates || !p) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+  return pgsvt_denoise_ex(X, dtype, nrows, ncols, nframes, Y, estimates, p, nullptr, st);
+}
+
+int pgsvt_denoise_batch(const pgsvt_sequence* seqs, uint32_t nseq, uint32_t slots,
+                        pgsvt_status* st) {
+  return guarded(st, [&](Stats& total) {
+    if (!seqs && nseq) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    for (uint32_t i = 0; i < nseq; ++i)
+      if (!seqs[i].X || !seqs[i].Y || !seqs[i].estimates || !seqs[i].params)
+        throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer in sequence " + std::to_string(i));
+    if (nseq == 0) return;
     need_device();
-    const size_t es = dtype_size(dtype);
-    validate(*p, nrows, ncols, nframes);
-    const size_t n = (size_t)nrows * ncols * nframes;
+    int dev = 0;
+    PGSVT_CK(cudaGetDevice(&dev));
+    // largest first, so the queue's tail holds the short sequences
+    std::vector<uint32_t> order(nseq);
+    for (uint32_t i = 0; i < nseq; ++i) order[i] = i;
+    auto cost = [&](uint32_t i) {
+      const pgsvt_sequence& q = seqs[i];
+      return (double)q.nrows * q.ncols * q.nframes * (double)q.params->block_size;
+    };
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
+    const int nw = (int)std::min<uint32_t>(nseq, slots ? slots : 2);
+    std::atomic<uint32_t> next{0};
+    std::vector<Stats> part(nw);
+    std::vector<int> codes(nseq, PGSVT_OK), cudas(nseq, 0);
+    std::vector<std::string> msgs(nseq);
+    auto worker = [&](int wi) {
+      cudaSetDevice(dev);
+      for (;;) {
+        const uint32_t k = next.fetch_add(1);
+        if (k >= nseq) break;
+        const uint32_t i = order[k];
+        const pgsvt_sequence& q = seqs[i];
+        const int rc = guarded(q.status, [&](Stats& stats) {
+          denoise_host(q.X, q.dtype, q.nrows, q.ncols, q.nframes, q.Y, q.estimates, *q.params,
+                       nullptr, q.lambdas, (int)q.nlambdas, q.risks, stats);
+          Stats& P = part[wi];
+          P.launches += stats.launches;
+          P.h2d += stats.h2d;
+          P.d2h += stats.d2h;
+          P.evals += stats.evals;
+          P.windows += stats.windows;
+          P.svd_launches += stats.svd_launches;
+          P.svd_matrices += stats.svd_matrices;
+          P.arps_exact += stats.arps_exact;
+          P.svd_fp64 += stats.svd_fp64;
+          P.svd_sweeps += stats.svd_sweeps;
+          P.svd_tuned |= stats.svd_tuned;
+          for (int j = 0; j < 8; ++j) P.stage[j] += stats.stage[j];
+        });
+        codes[i] = rc;
+        if (rc != PGSVT_OK) msgs[i] = "sequence " + std::to_string(i) + ": " + g_err;
+      }
+    };
+    std::vector<std::thread> th;
+    for (int wi = 1; wi < nw; ++wi) th.emplace_back(worker, wi);
+    worker(0);
+    for (auto& t : th) t.join();
+    for (const Stats& P : part) {
+      total.launches += P.launches;
+      total.h2d += P.h2d;
+      total.d2h += P.d2h;
+      total.evals += P.evals;
+      total.windows += P.windows;
+      total.svd_launches += P.svd_launches;
+      total.svd_matrices += P.svd_matrices;
+      total.arps_exact += P.arps_exact;
+      total.svd_fp64 += P.svd_fp64;
+      total.svd_sweeps += P.svd_sweeps;
+      total.svd_tuned |= P.svd_tuned;
+      for (int j = 0; j < 8; ++j) total.stage[j] += P.stage[j];
+    }
+    for (uint32_t i = 0; i < nseq; ++i)
+      if (codes[i] != PGSVT_OK) throw Fail(codes[i], msgs[i]);
+  });
+}
+
+// ---- learned lambda proposal: inference, gradient and training on the device
+
+int pgsvt_lambda_predict(const float* model, const float* features, uint32_t n, float* y) {
+  return guarded(nullptr, [&](Stats& stats) {
+    if (!model || !features || !y) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (n == 0) return;
+    need_device();
     DevMem mem;
     cudaStream_t s;
     PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
-    void* Xd = mem.get(n * es);
-    double* Yd = mem.arr<double>(n);
-    double* Ed = mem.arr<double>((size_t)nframes * 4);
-    PGSVT_CK(cudaMemcpyAsync(Xd, X, n * es, cudaMemcpyHostToDevice, s));
-    stats.h2d += n * es;
-    run_sequence(Xd, dtype, (int)nrows, (int)nframes, Yd, Ed, *p, s, stats);
-    PGSVT_CK(cudaMemcpyAsync(Y, Yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    PGSVT_CK(cudaMemcpyAsync(estimates, Ed, (size_t)nframes * 4 * sizeof(double),
-                             cudaMemcpyDeviceToHost, s));
+    float* m = mem.arr<float>(PGSVT_LAMBDA_MODEL_FLOATS);
+    void* wbf = mem.get(PGSVT_LAMBDA_MODEL_FLOATS * 2);
+    float* f = mem.arr<float>((size_t)n * PGSVT_LAMBDA_FEATURES);
+    float* yd = mem.arr<float>(n);
+    PGSVT_CK(cudaMemcpyAsync(m, model, sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(f, features, sizeof(float) * n * PGSVT_LAMBDA_FEATURES,
+                             cudaMemcpyHostToDevice, s));
+    PGSVT_CK(lambda_attrs());
+    check_launch(lambda_shadow(m, wbf, s), stats);
+    check_launch(lambda_forward(m, wbf, f, (int)n, yd, s), stats);
+    PGSVT_CK(cudaMemcpyAsync(y, yd, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     PGSVT_CK(cudaStreamSynchronize(s));
-    stats.d2h += n * sizeof(double) + (size_t)nframes * 4 * sizeof(double);
+  });
+}
+
+int pgsvt_lambda_grad(const float* model, const float* features, const float* targets, uint32_t n,
+                      float* grad, double* loss) {
+  return guarded(nullptr, [&](Stats& stats) {
+    if (!model || !features || !targets || !grad) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (n == 0) throw Fail(PGSVT_ERR_INVALID_ARG, "no samples");
+    need_device();
+    DevMem mem;
+    cudaStream_t s;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    const int nblk = ((int)n + 31) / 32;
+    float* m = mem.arr<float>(PGSVT_LAMBDA_MODEL_FLOATS);
+    void* wbf = mem.get(PGSVT_LAMBDA_MODEL_FLOATS * 2);
+    float* f = mem.arr<float>((size_t)n * PGSVT_LAMBDA_FEATURES);
+    float* t = mem.arr<float>(n);
+    float* part = mem.arr<float>((size_t)nblk * PGSVT_LAMBDA_PARAMS);
+    float* pl = mem.arr<float>(nblk);
+    float* g = mem.arr<float>(PGSVT_LAMBDA_PARAMS);
+    PGSVT_CK(cudaMemcpyAsync(m, model, sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(f, features, sizeof(float) * n * PGSVT_LAMBDA_FEATURES,
+                             cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(t, targets, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(lambda_attrs());
+    check_launch(lambda_shadow(m, wbf, s), stats);
+    check_launch(lambda_grad(m, wbf, f, t, (int)n, part, pl, g, s), stats, 2);
+    std::vector<float> hl(nblk);
+    PGSVT_CK(cudaMemcpyAsync(grad, g, sizeof(float) * PGSVT_LAMBDA_PARAMS, cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaMemcpyAsync(hl.data(), pl, sizeof(float) * nblk, cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    if (loss) {
+      double L = 0.0;
+      for (float v : hl) L += v;
+      *loss = L / n;
+    }
+  });
+}
+
+int pgsvt_lambda_train(float* model, const float* features, const float* targets, uint32_t n,
+                       const pgsvt_train_params* tp, float* epoch_loss, pgsvt_status* st) {
+  return guarded(st, [&](Stats& stats) {
+    if (!model || !features || !targets || !tp) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    const int batch = (int)tp->batch;
+    if (batch < 32 || batch % 32 != 0 || batch > 8192)
+      throw Fail(PGSVT_ERR_INVALID_ARG, "batch must be a multiple of 32 in [32, 8192]");
+    if (n < (uint32_t)batch) throw Fail(PGSVT_ERR_INVALID_ARG, "fewer samples than one batch");
+    if (tp->epochs < 1 || (uint64_t)tp->epochs * n > (1ull << 31))
+      throw Fail(PGSVT_ERR_INVALID_ARG, "epochs x samples must be in [1, 2^31]");
+    need_device();
+    DevMem mem;
+    cudaStream_t s;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    LambdaTrain t{};
+    t.n = (int)n;
+    t.batch = batch;
+    t.steps = (int)n / batch;
+    t.total_steps = t.steps * (int)tp->epochs;
+    t.lr = tp->lr;
+    t.lr_final = tp->lr_final;
+    t.wd = tp->weight_decay;
+    t.b1 = tp->beta1;
+    t.b2 = tp->beta2;
+    t.eps = tp->eps;
+    const int nblk = batch / 32;
+    t.m = mem.arr<float>(PGSVT_LAMBDA_MODEL_FLOATS);
+    t.wbf = mem.get(PGSVT_LAMBDA_MODEL_FLOATS * 2);
+    t.mom1 = mem.arr<float>(PGSVT_LAMBDA_PARAMS);
+    t.mom2 = mem.arr<float>(PGSVT_LAMBDA_PARAMS);
+    float* feat = mem.arr<float>((size_t)n * PGSVT_LAMBDA_FEATURES);
+    float* target = mem.arr<float>(n);
+    int32_t* perm = mem.arr<int32_t>((size_t)tp->epochs * n);
+    t.feat = feat;
+    t.target = target;
+    t.perm = perm;
+    t.epoch = mem.arr<int>(1);
+    t.part = mem.arr<float>((size_t)nblk * PGSVT_LAMBDA_PARAMS);
+    t.loss_acc = mem.arr<float>((size_t)t.steps * nblk);
+    t.epoch_loss = mem.arr<float>(tp->epochs);
+    // sample order of every epoch: Fisher-Yates shuffles from a pcg64 stream
+    std::vector<int32_t> hp((size_t)tp->epochs * n);
+    Pcg64 rng((Pcg64::u128)tp->seed);
+    for (uint32_t e = 0; e < tp->epochs; ++e) {
+      int32_t* q = hp.data() + (size_t)e * n;
+      for (uint32_t i = 0; i < n; ++i) q[i] = (int32_t)i;
+      for (uint32_t i = n - 1; i > 0; --i) {
+        const uint32_t j = (uint32_t)(((unsigned __int128)rng() * (i + 1)) >> 64);
+        std::swap(q[i], q[j]);
+      }
+    }
+    PGSVT_CK(cudaMemcpyAsync(t.m, model, sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(feat, features, sizeof(float) * n * PGSVT_LAMBDA_FEATURES,
+                             cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(target, targets, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    PGSVT_CK(cudaMemcpyAsync(perm, hp.data(), sizeof(int32_t) * hp.size(), cudaMemcpyHostToDevice, s));
+    stats.h2d += sizeof(float) * (PGSVT_LAMBDA_MODEL_FLOATS + (size_t)n * (PGSVT_LAMBDA_FEATURES + 1)) +
+                 sizeof(int32_t) * hp.size();
+    PGSVT_CK(cudaMemsetAsync(t.mom1, 0, sizeof(float) * PGSVT_LAMBDA_PARAMS, s));
+    PGSVT_CK(cudaMemsetAsync(t.mom2, 0, sizeof(float) * PGSVT_LAMBDA_PARAMS, s));
+    PGSVT_CK(cudaMemsetAsync(t.epoch, 0, sizeof(int), s));
+    PGSVT_CK(lambda_attrs());
+    check_launch(lambda_shadow(t.m, t.wbf, s), stats);
+    // one epoch = steps x (gradient, AdamW) + epoch bookkeeping, as a graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    PGSVT_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t ce = lambda_train_epoch(t, s);
+    const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    struct GG {
+      cudaGraph_t& g;
+      cudaGraphExec_t& x;
+      ~GG() {
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+      }
+    } gg{graph, exec};
+    PGSVT_CK(ce);
+    PGSVT_CK(ee);
+    PGSVT_CK(cudaGraphInstantiate(&exec, graph, 0));
+    for (uint32_t e = 0; e < tp->epochs; ++e) {
+      PGSVT_CK(cudaGraphLaunch(exec, s));
+      stats.launches += 2 * (uint64_t)t.steps + 1;
+    }
+    PGSVT_CK(cudaMemcpyAsync(model, t.m, sizeof(float) * PGSVT_LAMBDA_MODEL_FLOATS, cudaMemcpyDeviceToHost, s));
+    if (epoch_loss)
+      PGSVT_CK(cudaMemcpyAsync(epoch_loss, t.epoch_loss, sizeof(float) * tp->epochs,
+                               cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    stats.d2h += sizeof(float) * (PGSVT_LAMBDA_MODEL_FLOATS + (epoch_loss ? tp->epochs : 0));
+  });
+}
+
+int pgsvt_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nrows, uint32_t ncols,
+                        uint32_t nframes, uint32_t r) {
+  return guarded(nullptr, [&](Stats& stats) {
+    if (!src || !dst) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (nrows != ncols) throw Fail(PGSVT_ERR_INVALID_ARG, "frames must be square");
+    if (r < 1 || r > (uint32_t)kMaxMedian || 2 * r + 1 > nrows)
+      throw Fail(PGSVT_ERR_INVALID_ARG, "median radius must be in [1, 15] and 2r+1 <= frame side");
+    if (nframes == 0) return;
+    need_device();
+    const size_t F = (size_t)nrows * ncols, n = F * nframes;
+    DevMem mem;
+    cudaStream_t s;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    uint16_t* in = mem.arr<uint16_t>(n);
+    float* xs = mem.arr<float>(n);
+    float* zs = mem.arr<float>(n);
+    PGSVT_CK(cudaMemcpyAsync(in, src, n * 2, cudaMemcpyHostToDevice, s));
+    check_launch(launch_convert(in, PGSVT_U16, n, xs, nullptr, s), stats);
+    check_launch(launch_median(xs, nullptr, (int)nframes, (int)nrows, (int)r, zs, s), stats);
+    std::vector<float> h(n);
+    PGSVT_CK(cudaMemcpyAsync(h.data(), zs, n * 4, cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < n; ++i) dst[i] = (uint16_t)h[i];
   });
 }
 

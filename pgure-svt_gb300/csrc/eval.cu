@@ -100,8 +100,11 @@ __global__ void k_sum_u(Problem pb, DeviceBuffers d, int nblk) {
 // Bracketed batch grid search, identical to the oracle's: round 0 places K
 // points geometrically over [lo, hi]; each later round places K points evenly
 // inside the bracket formed by the neighbours of the best point so far.  A
-// hint (learned proposal) searches [hint/span, hint*span] first and falls back
-// to the plain search when its best point lies on that grid's edge.
+// hint (a given or learned proposal) runs a narrow search first: hint_K
+// points over [hint/span, hint*span] and hint_rounds refinements.  When the
+// best point of its grid lies on an edge and the neighbouring point's risk
+// is more than hint_flat (relative) above it, the plain search runs instead
+// and the better of the two results is kept.
 
 struct Sch {
   __device__ static void grid(SearchState& s, double lo, double hi) {
@@ -132,6 +135,17 @@ struct Sch {
   }
 };
 
+// The narrow grid inherits the plain search's bounds: a grid reaching below
+// the plain grid's bottom (upper * 1e-4) may refine down to 0 as the plain
+// search does, and a grid clipped at `upper` ends there as the plain one
+// does; a best point on such a bound is a result, not a miss.
+__device__ void start_narrow(SearchState& s, const Problem& pb, double upper, double hint) {
+  const double h = fmin(hint, upper);
+  const double lo = h / pb.hint_span;
+  Sch::phase(s, 1, pb.hint_K, pb.max_evals, pb.hint_rounds, lo <= upper * 1e-4 ? 1 : 0);
+  Sch::grid(s, lo, fmin(upper, h * pb.hint_span));
+}
+
 __global__ void k_search_init(Problem pb, DeviceBuffers d) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= pb.W) return;
@@ -156,13 +170,28 @@ __global__ void k_search_init(Problem pb, DeviceBuffers d) {
   wc.start = start;
   wc.upper = fmax(100.0, start);
   s.done = 0;
-  if (pb.hint > 0) {
-    Sch::phase(s, 1, pb.K, pb.max_evals, max(1, pb.rounds / 2), 0);
-    Sch::grid(s, pb.hint / pb.hint_span, fmin(wc.upper, pb.hint * pb.hint_span));
+  if (pb.nfixed > 0) {  // a given list: one round, no refinement
+    Sch::phase(s, 0, pb.nfixed, pb.nfixed, 0, 0);
+    for (int j = 0; j < pb.nfixed; ++j) s.next[j] = pb.fixed[j];
+    s.nnext = pb.nfixed;
+    s.first = 1;
+  } else if (pb.hint > 0) {
+    start_narrow(s, pb, wc.upper, pb.hint);
   } else {
     Sch::phase(s, 0, pb.K, pb.max_evals, pb.rounds, 1);
     Sch::grid(s, wc.upper * 1e-4, wc.upper);
   }
+}
+
+// Narrow searches around the learned proposals y = log10(lambda/upper).
+__global__ void k_search_hint(Problem pb, DeviceBuffers d) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= pb.W) return;
+  SearchState& s = d.st[w];
+  if (s.done) return;
+  const double upper = d.wc[w].upper;
+  const double y = fmin(0.0, fmax(-6.0, (double)d.prop[w]));  // NaN -> -6
+  start_narrow(s, pb, upper, upper * pow(10.0, y));
 }
 
 __device__ void search_finish(SearchState& s, unsigned long long* counters) {
@@ -234,8 +263,14 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
   s.best = b;
   if (s.first) {
     s.first = 0;
-    const bool edge = (b == 0 || b == s.npts - 1);
-    if (s.phase == 1 && edge) {  // proposal not bracketed: plain search
+    const bool bound = (b == 0 && s.zero_lo) || (b == s.npts - 1 && s.lam[b] >= wc.upper);
+    const bool edge = (b == 0 || b == s.npts - 1) && !bound;
+    bool steep = edge;
+    if (edge && s.npts >= 2) {
+      const int nb = (b == 0) ? 1 : s.npts - 2;
+      steep = !(s.risk[nb] - s.risk[b] <= pb.hint_flat * fabs(s.risk[b]));
+    }
+    if (s.phase == 1 && steep) {  // proposal not bracketed: plain search
       s.hint_lambda = s.lam[b];
       s.hint_risk = s.risk[b];
       const int left = pb.max_evals > s.evals_phase ? pb.max_evals - s.evals_phase : 1;
@@ -516,6 +551,17 @@ __global__ void k_output(Problem pb, DeviceBuffers d) {
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int n = g.nimg;
+    if (d.risk_out) d.risk_out[wc.t] = d.st[w].final_risk;
+    if (pb.fixed_risk) {  // risks of the given list, in its order
+      const SearchState& s = d.st[w];
+      for (int j = 0; j < pb.nfixed; ++j) {
+        double r = NAN;
+        for (int i = 0; i < s.npts; ++i)
+          if (s.lam[i] == pb.fixed[j]) r = s.risk[i];
+        pb.fixed_risk[(size_t)wc.t * pb.nfixed + j] = r;
+      }
+    }
+    if (d.evals_out) d.evals_out[wc.t] = (uint32_t)d.st[w].evals_total;
     d.est[wc.t] = d.st[w].final_lambda;
     d.est[wc.t + n] = pb.alpha_c;
     d.est[wc.t + 2 * (size_t)n] = pb.mu_c;
@@ -624,6 +670,11 @@ cudaError_t launch_fields(const Problem& pb, const DeviceBuffers& d, cudaStream_
 
 cudaError_t launch_search_init(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   k_search_init<<<(pb.W + 63) / 64, 64, 0, s>>>(pb, d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_search_hint(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+  k_search_hint<<<(pb.W + 63) / 64, 64, 0, s>>>(pb, d);
   return cudaGetLastError();
 }
 

@@ -62,6 +62,8 @@ __device__ __forceinline__ float unfix32(long long a) {
 // Per-window constants, computed on the device.
 struct WinConst {
   double umax;     // window maximum (pguresvt.hpp:116)
+  double wnorm;    // maximum of the median-filtered window (ARPS input
+                   // scale, pguresvt.hpp:117; 1 when it is 0)
   double unorm;    // divisor of the normalisation: umax, or 1 for an all-zero
                    // window (the reference's 0/0 ends as a zero output frame)
   double sum_u;    // accu(u)
@@ -120,13 +122,22 @@ struct Problem {
   double tol;
   int max_evals, rounds;
   double hint, hint_span;
+  int hint_K, hint_rounds;  // narrow search: points per round, refinements
+  double hint_flat;         // relative risk within which an edge best is kept
   int acc64;             // accumulators int64 at 2^-32 (else int32 at 2^-20)
+  int svd_variant;       // kernel shape of the SVD (svd.cu)
+  const double* fixed;   // device list of lambda values evaluated once per
+  int nfixed;            // window instead of a search (null / 0: search)
+  double* fixed_risk;    // optional out [nimg][nfixed], frame-major
 };
 
 struct DeviceBuffers {
   const float* xs;
   const double* x64;
   const double* fmax;      // per input frame maximum
+  const float* zs;         // median-filtered sequence (null: no pre-filter)
+  const double* zmax;      // its per-frame maxima
+  float* wz;               // [W][nwin][S*S] ARPS input zs / wnorm
   float* u;
   uint32_t* pos;
   const int32_t* plist;    // kept patch -> position index
@@ -155,6 +166,17 @@ struct DeviceBuffers {
   double* est;             // output estimates (nimg x 4)
   unsigned long long* counters;  // [0] ARPS FP64 steps, [1] SVD warp-sweeps,
                                  // [2] FP64 convergence tests, [3] risk evaluations
+  // learned lambda proposal
+  const int32_t* feat_slots;  // sampled kept-patch slots of the features
+  int nfeat_slots;
+  float* feat;             // [W][67] window features
+  float* prop;             // [W] proposals y = log10(lambda/upper)
+  const float* model;      // FP32 model (null: no proposal)
+  const void* model_bf16;  // its bf16 shadow
+  float* feat_out;         // optional per-frame outputs (device, frame-indexed)
+  float* prop_out;
+  double* risk_out;
+  uint32_t* evals_out;
   int win0;                // first window (output frame) of this batch
   int ncopies;             // SVD copies decomposed (1, 3 or 4)
   int nblk_eval, nblk_mse;
@@ -165,6 +187,9 @@ cudaError_t launch_convert(const void* X, int dtype, size_t n, float* xs, double
                            cudaStream_t s);
 cudaError_t launch_frame_max(const float* xs, const double* x64, int nimg, size_t F,
                              double* fmax, cudaStream_t s);
+cudaError_t launch_median(const float* xs, const double* x64, int nimg, int S, int r, float* zs,
+                          cudaStream_t s);
+constexpr int kMaxMedian = 15;     // median pre-filter radius supported
 cudaError_t launch_window_setup(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 cudaError_t launch_window_norm_only(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 cudaError_t launch_arps(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
@@ -179,12 +204,39 @@ cudaError_t launch_cube_out(const Problem& pb, const DeviceBuffers& d, double* v
 cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double* out,
                               cudaStream_t s);
 
+// learned lambda proposal (lambda.cu)
+struct LambdaTrain {
+  float* m;            // FP32 model (PGSVT_LAMBDA_MODEL_FLOATS)
+  void* wbf;           // bf16 shadow
+  float *mom1, *mom2;  // Adam moments (PGSVT_LAMBDA_PARAMS)
+  const float* feat;   // [n][67]
+  const float* target; // [n]
+  const int32_t* perm; // [epochs][n] sample order
+  int* epoch;          // device epoch counter
+  float* part;         // [batch/32][PGSVT_LAMBDA_PARAMS] gradient partials
+  float* loss_acc;     // [steps][batch/32]
+  float* epoch_loss;   // [epochs]
+  int n, batch, steps, total_steps;
+  float lr, lr_final, wd, b1, b2, eps;
+};
+cudaError_t launch_lambda_features(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_lambda_propose(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t launch_search_hint(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t lambda_shadow(const float* m, void* wbf, cudaStream_t s);
+cudaError_t lambda_forward(const float* m, const void* wbf, const float* feat, int n, float* y,
+                           cudaStream_t s);
+cudaError_t lambda_grad(const float* m, const void* wbf, const float* feat, const float* target,
+                        int n, float* part, float* part_loss, float* grad, cudaStream_t s);
+cudaError_t lambda_train_epoch(const LambdaTrain& t, cudaStream_t s);
+cudaError_t lambda_attrs();
+
 // message returned by pgsvt_last_error() on the calling thread
 void set_last_error(const std::string& m);
 
 int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
 int svd_columns(int nwin);
+int svd_variants(int M);
 bool svd_supported(int bs, int nwin);
 
 }  // namespace pgsvt

@@ -65,6 +65,63 @@ cudaError_t launch_frame_max(const float* xs, const double* x64, int nimg, size_
   return cudaGetLastError();
 }
 
+// ---- median pre-filter of the ARPS input (pguresvt.hpp:69-84)
+//
+// The reference converts each frame to uint16 (arma::conv_to; taken here as
+// C's truncation toward zero, clamped to [0, 65535]) and filters it with
+// ConstantTimeMedianFilter (medfilter.hpp:478-541) of radius r, which is the
+// exact median of the (2r+1)^2 window with coordinates clamped to the frame.
+// GB300 form: one thread per output pixel of a 32 x 8 tile, the tile and its
+// halo staged in shared memory as uint16; the median is found by a 16-step
+// binary search on the value (the largest v with #{x < v} <= n/2), each step
+// one counting pass over the window.
+__device__ __forceinline__ uint16_t to_u16(double v) {
+  if (!(v > 0.0)) return 0;
+  if (v >= 65535.0) return 65535;
+  return (uint16_t)v;
+}
+
+template <bool F64>
+__global__ void __launch_bounds__(256) k_median(const float* __restrict__ xs,
+                                                const double* __restrict__ x64, int S, int r,
+                                                float* __restrict__ zs) {
+  extern __shared__ uint16_t tile[];
+  const size_t base = (size_t)blockIdx.z * S * S;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;  // x: the fast axis
+  const int TW = 32 + 2 * r, TH = 8 + 2 * r;
+  for (int i = threadIdx.x; i < TW * TH; i += blockDim.x) {
+    const int gx = min(max(x0 + i % TW - r, 0), S - 1);
+    const int gy = min(max(y0 + i / TW - r, 0), S - 1);
+    const size_t k = base + gx + (size_t)gy * S;
+    tile[i] = to_u16(F64 ? x64[k] : (double)xs[k]);
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (x0 + tx >= S || y0 + ty >= S) return;
+  const int d = 2 * r + 1, half = (d * d) / 2;
+  uint32_t ans = 0;
+  for (int b = 15; b >= 0; --b) {
+    const uint32_t cand = ans | (1u << b);
+    int cnt = 0;
+    for (int dy = 0; dy < d; ++dy) {
+      const uint16_t* row = tile + (ty + dy) * TW + tx;
+      for (int dx = 0; dx < d; ++dx) cnt += (uint32_t)row[dx] < cand;
+    }
+    if (cnt <= half) ans = cand;
+  }
+  zs[base + (x0 + tx) + (size_t)(y0 + ty) * S] = (float)ans;
+}
+
+cudaError_t launch_median(const float* xs, const double* x64, int nimg, int S, int r, float* zs,
+                          cudaStream_t s) {
+  if (r < 0 || r > kMaxMedian) return cudaErrorInvalidValue;
+  const dim3 grid((S + 31) / 32, (S + 7) / 8, nimg);
+  const size_t shm = (size_t)(32 + 2 * r) * (8 + 2 * r) * sizeof(uint16_t);
+  if (x64) k_median<true><<<grid, 256, shm, s>>>(xs, x64, S, r, zs);
+  else k_median<false><<<grid, 256, shm, s>>>(xs, x64, S, r, zs);
+  return cudaGetLastError();
+}
+
 // Window constants and the normalised window u = x / umax.
 __global__ void k_window_const(Problem pb, DeviceBuffers d) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,6 +137,12 @@ __global__ void k_window_const(Problem pb, DeviceBuffers d) {
   WinConst c;
   c.umax = umax;
   c.unorm = umax > 0.0 ? umax : 1.0;
+  c.wnorm = c.unorm;
+  if (d.zs) {
+    double wm = d.zmax[s0];
+    for (int k = 1; k < g.nwin; ++k) wm = fmax(wm, d.zmax[s0 + k]);
+    c.wnorm = wm > 0.0 ? wm : 1.0;
+  }
   c.t = t;
   c.s0 = s0;
   if (t < g.fw) {
@@ -124,6 +187,13 @@ __global__ void k_window_norm(Problem pb, DeviceBuffers d) {
        i += (size_t)gridDim.x * blockDim.x) {
     if (F64) u[i] = (float)(d.x64[base + i] / c.unorm);
     else u[i] = __fdiv_rn(d.xs[base + i], um);  // exact operands: correctly rounded
+  }
+  if (d.zs) {  // ARPS input from the median-filtered sequence
+    float* wz = d.wz + (size_t)w * C;
+    const float wn = (float)c.wnorm;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < C;
+         i += (size_t)gridDim.x * blockDim.x)
+      wz[i] = __fdiv_rn(d.zs[base + i], wn);
   }
 }
 

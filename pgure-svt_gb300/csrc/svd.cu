@@ -43,10 +43,21 @@ bool svd_supported(int bs, int nwin) {
 
 // Kernel shapes: rows per lane x lanes per patch covers bs*bs rows; the
 // instantiations live in svd_i*.cu so that they compile in parallel.
+// Variant 0 is the default shape of each patch size; variant 1 spreads a
+// patch over more lanes (fewer registers per lane, more shuffles per inner
+// product).  Both give the same results up to FP32 rounding; the autotuner
+// (capi.cu) times them on the caller's data and keeps the faster one.
+int svd_variants(int M) { return (M > 16 && M <= 32) ? 1 : 2; }
+
 cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   using namespace svdk;
   const int M = pb.g.M, NC = pb.g.NC;
+  const bool alt = pb.svd_variant == 1;
   if (M <= 16) {  // bs 2..4
+    if (alt) {
+      if (NC == 10) return run_svd<2, 8, 10>(pb, d, s);
+      if (NC == 16) return run_svd<2, 8, 16>(pb, d, s);
+    }
     if (NC == 10) return run_svd<4, 4, 10>(pb, d, s);
     if (NC == 16) return run_svd<4, 4, 16>(pb, d, s);
   } else if (M <= 32) {  // bs 5
@@ -54,10 +65,20 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
     if (NC == 16) return run_svd<4, 8, 16>(pb, d, s);
     if (NC == 22) return run_svd<4, 8, 22>(pb, d, s);
   } else if (M <= 40) {  // bs 6
+    if (alt) {
+      if (NC == 10) return run_svd<3, 16, 10>(pb, d, s);
+      if (NC == 16) return run_svd<3, 16, 16>(pb, d, s);
+      if (NC == 22) return run_svd<3, 16, 22>(pb, d, s);
+    }
     if (NC == 10) return run_svd<5, 8, 10>(pb, d, s);
     if (NC == 16) return run_svd<5, 8, 16>(pb, d, s);
     if (NC == 22) return run_svd<5, 8, 22>(pb, d, s);
   } else {  // bs 7, 8
+    if (alt) {
+      if (NC == 10) return run_svd<2, 32, 10>(pb, d, s);
+      if (NC == 16) return run_svd<2, 32, 16>(pb, d, s);
+      if (NC == 22) return run_svd<2, 32, 22>(pb, d, s);
+    }
     if (NC == 10) return run_svd<4, 16, 10>(pb, d, s);
     if (NC == 16) return run_svd<4, 16, 16>(pb, d, s);
     if (NC == 22) return run_svd<4, 16, 22>(pb, d, s);

@@ -1,0 +1,116 @@
+"""Train the learned lambda proposal and write the shipped model.
+
+    python pgure-svt_gb300/train_lambda.py --sequences 2000 --held-out 20 \\
+        --out pgure-svt_gb300/lambda_mlp.npz --report lambda_report.json
+
+Steps (all compute on the GPU through libpgsvt.so):
+1. label: for each seeded random sequence (learned.random_sequence), the plain
+   PGURE search of windows 7..10 gives (features, log10(lambda*/100));
+2. train: pgsvt_lambda_train (bf16 weights, FP32 accumulation, AdamW,
+   one CUDA graph per epoch) from learned.init_model;
+3. evaluate on held-out sequences: prediction error, and plain vs learned
+   search (risk evaluations and risk gap per window).
+Sequences are generated by a spawn process pool started before the first
+GPU call.
+"""
+import argparse
+import importlib.util
+import json
+import multiprocessing as mp
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _package():
+    if "pguresvt_gb300" in sys.modules:
+        return sys.modules["pguresvt_gb300"]
+    spec = importlib.util.spec_from_file_location(
+        "pguresvt_gb300", os.path.join(HERE, "__init__.py"), submodule_search_locations=[HERE])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["pguresvt_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _gen(seed):  # pool worker: the package is imported per process
+    return _package().learned.random_sequence(seed)
+
+
+def evaluate(pkg, model, seeds, pool):
+    """Held-out windows: prediction error, plain vs learned search."""
+    L = pkg.learned
+    rows = []
+    for noisy, noise in pool.imap(_gen, seeds):
+        lab = L.label(noisy, noise)
+        res = L.compare(noisy, noise, model, frames=L.LABEL_FRAMES)
+        f0, f1 = L.LABEL_FRAMES
+        pl, le = res["plain"], res["learned"]
+        for t in range(f0, f1):
+            rp, rl = pl["risk"][t], le["risk"][t]
+            rows.append(dict(side=int(noisy.shape[0]), y=float(lab["targets"][t - f0]),
+                             y_hat=float(le["proposals"][t]), evals_plain=int(pl["evals"][t]),
+                             evals_learned=int(le["evals"][t]),
+                             risk_gap=float((rl - rp) / abs(rp)) if rp != 0 else 0.0))
+    y = np.array([r["y"] for r in rows])
+    yh = np.array([r["y_hat"] for r in rows])
+    ep = np.array([r["evals_plain"] for r in rows])
+    el = np.array([r["evals_learned"] for r in rows])
+    gap = np.array([r["risk_gap"] for r in rows])
+    return dict(windows=len(rows), rmse_log10=float(np.sqrt(np.mean((y - yh) ** 2))),
+                evals_plain=float(ep.mean()), evals_learned=float(el.mean()),
+                fallbacks=int(np.sum(el > 2 * 4 + 0)), risk_gap_max=float(gap.max()),
+                risk_gap_mean=float(gap.mean()), frac_gap_le_1pct=float(np.mean(gap <= 0.01)))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--sequences", type=int, default=2000)
+    ap.add_argument("--held-out", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=600)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--workers", type=int, default=max(1, min(12, (os.cpu_count() or 2) - 2)))
+    ap.add_argument("--out", default=os.path.join(HERE, "lambda_mlp.npz"))
+    ap.add_argument("--data", default=None, help="also save the labelled set (.npz)")
+    ap.add_argument("--report", default=None)
+    a = ap.parse_args()
+
+    pool = mp.get_context("spawn").Pool(a.workers)  # before any GPU call
+    pkg = _package()
+    L = pkg.learned
+    t0 = time.time()
+    seeds = [a.seed * 1000003 + i for i in range(a.sequences)]
+    parts = [L.label(noisy, noise) for noisy, noise in pool.imap(_gen, seeds, chunksize=2)]
+    data = {k: np.concatenate([q[k] for q in parts]) for k in parts[0]}
+    t_label = time.time() - t0
+    if a.data:
+        np.savez_compressed(a.data, **data)
+    t1 = time.time()
+    model, curve = L.train(data["features"], data["targets"], epochs=a.epochs, batch=a.batch,
+                           seed=a.seed, lr=a.lr)
+    t_train = time.time() - t1
+    held = [10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out)]
+    ev = evaluate(pkg, model, held, pool) if a.held_out else {}
+    pool.close()
+    pool.join()
+    L.save_model(model, a.out, n_train=len(data["targets"]), epochs=a.epochs,
+                 final_loss=float(curve[-1]), seed=a.seed)
+    rep = dict(train_windows=int(len(data["targets"])), label_seconds=t_label,
+               train_seconds=t_train, epochs=a.epochs, loss_first=float(curve[0]),
+               loss_last=float(curve[-1]), target_mean=float(data["targets"].mean()),
+               target_std=float(data["targets"].std()),
+               plain_evals_mean=float(data["evals"].mean()), held_out=ev)
+    print(json.dumps(rep))
+    if a.report:
+        with open(a.report, "w") as f:
+            json.dump(rep, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -33,10 +33,23 @@ def test_version_and_defaults(capi):
 
 
 def test_params_layout_matches_oracle(capi, oracle):
-    # the oracle mirrors pgsvt_params field by field
-    assert [f[0] for f in capi.Params._fields_] == [f[0] for f in oracle.OrcParams._fields_]
-    import ctypes
-    assert ctypes.sizeof(capi.Params) == ctypes.sizeof(oracle.OrcParams)
+    # the oracle mirrors pgsvt_params field by field, then adds its own
+    # per-frame hint and output pointers
+    names = [f[0] for f in capi.Params._fields_]
+    assert names == [f[0] for f in oracle.OrcParams._fields_][:len(names)]
+    for n in names:
+        assert getattr(capi.Params, n).offset == getattr(oracle.OrcParams, n).offset
+
+
+def test_lambda_model_constants(capi):
+    text = open(os.path.join(ROOT, "include", "pgsvt.h")).read()
+    for name in ("LAMBDA_FEATURES", "LAMBDA_HIDDEN", "LAMBDA_SAMPLES", "LAMBDA_MODEL_FLOATS",
+                 "LAMBDA_PARAM_OFFSET", "LAMBDA_PARAMS"):
+        m = re.search(r"#define PGSVT_%s (\d+)" % name, text)
+        assert m and int(m.group(1)) == getattr(capi, name), name
+    H, F = capi.LAMBDA_HIDDEN, capi.LAMBDA_FEATURES
+    assert capi.LAMBDA_PARAMS == H * F + H + 2 * (H * H + H) + H + 1
+    assert capi.LAMBDA_MODEL_FLOATS == 2 * F + capi.LAMBDA_PARAMS + 2
 
 
 class TestErrors:

@@ -1,0 +1,102 @@
+"""Batches of uneven sequences (pgsvt_denoise_batch) and the SVD kernel
+shapes of the autotuner, against single-sequence calls and the FP64 oracle.
+
+Tolerances: a batch runs every sequence through the same kernels as a
+single call, so its outputs are identical; risks at fixed lambdas are FP64
+sums of FP32 terms and are compared with the oracle at 1e-4 relative (as the
+component risk tests); the two SVD kernel shapes round differently in FP32
+and agree to 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _seq(pkg, side, nt, seed, bs, T, lams=None):
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=seed, side=side, nt=nt)
+    return dict(X=noisy, bs=bs, T=T, noise=(a, m, s), lambdas=lams)
+
+
+def _params(capi, q, **kw):
+    a, m, s = q["noise"]
+    return capi.default_params(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s,
+                               block_size=q["bs"], traj_length=q["T"], **kw)
+
+
+def _batch(pkg, capi):
+    lam = np.array([0.01, 0.1, 1.0, 10.0])
+    return [_seq(pkg, 48, 20, 1, 4, 15, lam), _seq(pkg, 40, 12, 2, 6, 9, lam * 3),
+            _seq(pkg, 36, 24, 3, 8, 21, lam / 2), _seq(pkg, 32, 16, 4, 4, 15)]
+
+
+def test_batch_matches_single_calls(capi, pkg):
+    seqs = _batch(pkg, capi)
+    inp = [dict(X=q["X"], params=_params(capi, q), lambdas=q["lambdas"]) for q in seqs]
+    res, st = capi.denoise_batch(inp, slots=3)
+    assert st.code == 0 and st.windows == sum(q["X"].shape[2] for q in seqs)
+    for q, r in zip(inp, res):
+        one, _ = capi.denoise_batch([q], slots=1)
+        np.testing.assert_array_equal(r["Y"], one[0]["Y"])
+        np.testing.assert_array_equal(r["est"], one[0]["est"])
+        if q["lambdas"] is not None:
+            np.testing.assert_array_equal(r["risks"], one[0]["risks"])
+            # the output lambda is the list's value of least risk
+            best = np.asarray(q["lambdas"])[np.argmin(r["risks"], axis=1)]
+            np.testing.assert_array_equal(r["est"][:, 0], best)
+            assert r["status"].risk_evals == q["X"].shape[2] * len(q["lambdas"])
+
+
+def test_batch_fixed_lambda_risks_match_oracle(capi, pkg, oracle):
+    q = _batch(pkg, capi)[0]
+    res, _ = capi.denoise_batch([dict(X=q["X"], params=_params(capi, q),
+                                      lambdas=q["lambdas"])])
+    X = q["X"].astype(np.float64)
+    a, m, s = q["noise"]
+    for t in (0, 10, 19):
+        s0 = 0 if t < 7 else (X.shape[2] - 15 if t >= X.shape[2] - 7 else t - 7)
+        u = X[:, :, s0:s0 + 15]
+        u = u / u.max()
+        rows, cols = oracle.arps_window(u, 4, 7, t, 7, X.shape[2])
+        r0 = oracle.risk_window(u, 4, 1, rows, cols, q["lambdas"], a, m, s, 5)
+        np.testing.assert_allclose(res[0]["risks"][t], r0, rtol=1e-4, atol=1e-7)
+
+
+def test_batch_reports_errors_per_sequence(capi, pkg):
+    seqs = _batch(pkg, capi)[:2]
+    bad = dict(X=seqs[1]["X"][:, :20, :], params=_params(capi, seqs[1]))  # not square
+    good = dict(X=seqs[0]["X"], params=_params(capi, seqs[0]))
+    with pytest.raises(capi.PgsvtError, match="square"):
+        capi.denoise_batch([good, bad])
+
+
+@pytest.mark.parametrize("bs,T", [(4, 15), (6, 15), (8, 21)])
+def test_alternative_svd_shape_matches_oracle(capi, pkg, oracle, bs, T):
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=6, side=40, nt=T + 2)
+    X = noisy.astype(np.float64)
+    fr = (T // 2, T // 2 + 2)
+    base = dict(median_size=0, optimize_pgure=0, lambda_=0.5, block_size=bs, traj_length=T,
+                frame_begin=fr[0], frame_end=fr[1])
+    Y0, _, st0 = capi.denoise(X, capi.default_params(autotune=0, **base))
+    Y1, _, st1 = capi.denoise(X, capi.default_params(autotune=2, **base))
+    assert st0.svd_variant == 0 and st1.svd_variant == 1
+    Yo, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.5, block_size=bs,
+                              traj_length=T, frame_begin=fr[0], frame_end=fr[1], n_jobs=2)
+    f = slice(*fr)
+    scale = np.abs(Yo[:, :, f]).max()
+    for Y in (Y0, Y1):
+        assert np.abs(Y[:, :, f] - Yo[:, :, f]).max() <= 1e-4 * scale
+    assert np.abs(Y1[:, :, f] - Y0[:, :, f]).max() <= 1e-4 * scale
+
+
+def test_autotuner_picks_and_caches(capi, pkg):
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=7, side=64, nt=16)
+    p = capi.default_params(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, autotune=1,
+                            block_size=6, traj_length=9)
+    Y1, e1, st1 = capi.denoise(noisy, p)
+    Y2, e2, st2 = capi.denoise(noisy, p)
+    assert st1.svd_tuned == 1 and st2.svd_tuned == 0
+    assert st1.svd_variant == st2.svd_variant
+    # the tuned call's outputs are those of its chosen shape
+    np.testing.assert_array_equal(Y1, Y2)
+    np.testing.assert_array_equal(e1, e2)

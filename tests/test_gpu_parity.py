@@ -234,3 +234,25 @@ def test_frame_range_shards_sum_to_full_run(capi, pkg, g):
         assert not Yr[:, :, :b].any() and not Yr[:, :, e:].any()
         parts.append(Yr)
     np.testing.assert_array_equal(sum(parts), Y)
+
+
+# ---- median pre-filter of the ARPS input
+
+def test_median_filter_matches_reference_fixtures(capi):
+    z = np.load(os.path.join(GOLDEN, "median.npz"))
+    for k in range(int(z["n"])):
+        out = capi.median_filter(z["in_%d" % k], int(z["r_%d" % k]))
+        np.testing.assert_array_equal(out, z["out_%d" % k])
+
+
+def test_denoise_with_median_prefilter_matches_oracle(capi, oracle, g):
+    # fixed lambda: the output depends on the filter only through the ARPS
+    # trajectories, which must be the oracle's
+    X = g["X"].astype(np.float64) * 7.3  # non-integer values: the uint16 conversion truncates
+    p = capi.default_params(median_size=5, optimize_pgure=0, lambda_=0.1)
+    Y, est, st = capi.denoise(X, p)
+    Y0, _, _ = oracle.denoise(X, median_size=5, optimize_pgure=0, lambda_=0.1, n_jobs=4)
+    assert np.abs(Y - Y0).max() < 2e-5 * np.abs(Y0).max()
+    # and the filter changed the trajectories
+    Y1, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.1, n_jobs=4)
+    assert np.abs(Y1 - Y0).max() > 1e-3 * np.abs(Y0).max()

@@ -265,3 +265,30 @@ def test_reference_fixture_quality_bound(oracle):
                dict(optimize_pgure=1, alpha=0.1, mu=100.0, sigma=100.0, random_seed=101)):
         Yd, _, _ = oracle.denoise(Y, n_jobs=4, median_size=-1, **kw)
         assert _nsed(X, Yd) < 0.025
+
+
+# ---- median pre-filter (medfilter.hpp:478-541 via pguresvt.hpp:69-80)
+
+def test_median_restatement_matches_reference_fixtures(oracle):
+    z = np.load(os.path.join(GOLDEN, "median.npz"))
+    for k in range(int(z["n"])):
+        out = oracle.median_filter(z["in_%d" % k], int(z["r_%d" % k]))
+        np.testing.assert_array_equal(out, z["out_%d" % k])
+
+
+def test_median_restatement_matches_live_reference(oracle):
+    if not reference_available():
+        pytest.skip("reference tree absent")
+    import ctypes
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(GOLDEN), "..", "oracle"))
+    import build as obuild
+    L = ctypes.CDLL(obuild.build_ref_median())
+    L.ref_median_filter.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int]
+    rng = np.random.default_rng(7)
+    for S, r in [(16, 2), (27, 6), (50, 5), (31, 15)]:
+        a = np.asfortranarray(rng.integers(0, 2000, (S, S)).astype(np.uint16))
+        ref = np.zeros_like(a, order="F")
+        L.ref_median_filter(a.ctypes.data, ref.ctypes.data, S, S, r)
+        np.testing.assert_array_equal(oracle.median_filter(a, r), ref)
