@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles ``oracle/pgsvt_oracle.cpp`` with g++ into
+Compiles ``oracle/pgsvt_oracle.cpp`` and ``oracle/noise_oracle.cpp`` with g++ into
 ``oracle/_build/libpgsvt_oracle.so``.  ``-ffp-contract=off`` keeps the FP64
 arithmetic identical on x86_64 and aarch64 (no fused multiply-adds), so the
 oracle's ARPS costs and argmins are the same bits on both machines.
@@ -36,14 +36,15 @@ def _stale(target, sources):
 def build(force=False, verbose=False):
     """Compile the oracle shared library if it is missing or out of date."""
     src = os.path.join(HERE, "pgsvt_oracle.cpp")
+    src2 = os.path.join(HERE, "noise_oracle.cpp")
     hdr = os.path.join(HERE, "pgsvt_oracle.h")
-    if not force and not _stale(LIB, [src, hdr, __file__]):
+    if not force and not _stale(LIB, [src, src2, hdr, __file__]):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread",
            "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
-           "-o", tmp, src]
+           "-o", tmp, src, src2]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

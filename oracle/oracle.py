@@ -96,6 +96,8 @@ def lib():
             ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
             ctypes.c_double, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
             ctypes.c_void_p]
+        L.orc_noise_estimate.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 4 + [
+            P(ctypes.c_double)] * 3
         L.orc_median_filter.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3
         L.orc_denoise.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [
             P(OrcParams), ctypes.c_void_p, ctypes.c_void_p, P(OrcReport)]
@@ -199,6 +201,16 @@ def risk_window(u, bs, ov, rows, cols, lambdas, alpha, mu, sigma, seed, compat=C
                                  _ptr(np.ascontiguousarray(cols, np.int32)), alpha, mu, sigma, seed, compat,
                                  _ptr(lam), len(lam), _ptr(out)))
     return out
+
+
+def noise_estimate(u, method=4, alpha=-1.0, mu=-1.0, sigma=-1.0):
+    """NoiseEstimator::Estimate on a normalised window (rows, cols, slices);
+    returns (alpha, mu, sigma), given values (>= 0) kept."""
+    u = _cube(u)
+    a, m, s = ctypes.c_double(alpha), ctypes.c_double(mu), ctypes.c_double(sigma)
+    _check(lib().orc_noise_estimate(_ptr(u), u.shape[0], u.shape[1], u.shape[2], method,
+                                    ctypes.byref(a), ctypes.byref(m), ctypes.byref(s)))
+    return a.value, m.value, s.value
 
 
 def median_filter(frame, r):

@@ -35,6 +35,10 @@
 #include <thread>
 #include <vector>
 
+// noise_oracle.cpp: NoiseEstimator::Estimate (noise.hpp:36-152)
+void orc_noise_estimate_impl(const double* u, uint32_t ny, uint32_t nx, uint32_t T,
+                             uint32_t method, double& alpha, double& mu, double& sigma);
+
 namespace {
 
 thread_local std::string g_err;
@@ -669,8 +673,6 @@ void validate(const orc_params& p, uint32_t nrows, uint32_t ncols, uint32_t nimg
   if (p.motion_estimation && p.motion_window < 1) throw Fail(1, "motion_window must be >= 1");
   if (p.median_size > 0 && 2 * p.median_size + 1 > nrows)
     throw Fail(1, "median window wider than the frame (medfilter.hpp:347-348)");
-  if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0))
-    throw Fail(2, "noise estimation not restated in the oracle: give alpha, mu, sigma");
   if (!p.optimize_pgure && p.lambda < 0) throw Fail(1, "lambda must be >= 0 without optimisation");
 }
 
@@ -678,6 +680,7 @@ void validate(const orc_params& p, uint32_t nrows, uint32_t ncols, uint32_t nimg
 struct WindowOut {
   double lambda, risk;
   uint32_t evals;
+  double alpha, mu, sigma;  // noise parameters of the window (estimates(t, 1..3))
 };
 
 WindowOut run_window(const double* X, const double* Z, const orc_params& p, const Plan& pl,
@@ -697,15 +700,20 @@ WindowOut run_window(const double* X, const double* Z, const orc_params& p, cons
     for (double x : w) wmax = std::max(wmax, x);
     for (double& x : w) x /= wmax;
   }
+  // noise parameters: user values, the rest estimated on u when optimising
+  // (pguresvt.hpp:62-65,122-127)
+  double na = p.alpha >= 0 ? p.alpha : -1.0, nm = p.mu >= 0 ? p.mu : -1.0;
+  double ns = p.sigma >= 0 ? p.sigma : -1.0;
+  if (p.optimize_pgure)
+    orc_noise_estimate_impl(u.data(), g.S, g.S, g.nwin, p.noise_method, na, nm, ns);
   std::vector<int32_t> rows((size_t)g.P * g.nwin), cols((size_t)g.P * g.nwin);
   {
     Arps a(Z ? w.data() : u.data(), g, pl.mw, rows.data(), cols.data());
     a.estimate(t, pl.fw, pl.nimg, p.motion_estimation != 0, p.compat_flags & kCompatZeroMotion);
   }
-  Pgure pg(g, u.data(), patch_list(g.S, g.bs, pl.ov), rows.data(), cols.data(), p.alpha,
-           p.mu, p.sigma, p.random_seed, p.exp_weighting != 0, p.optimize_pgure != 0,
-           p.compat_flags);
-  WindowOut out{p.lambda, 0.0, 0};
+  Pgure pg(g, u.data(), patch_list(g.S, g.bs, pl.ov), rows.data(), cols.data(), na, nm, ns,
+           p.random_seed, p.exp_weighting != 0, p.optimize_pgure != 0, p.compat_flags);
+  WindowOut out{p.lambda, 0.0, 0, na, nm, ns};
   if (p.optimize_pgure) {
     const double OoN = 1.0 / (pl.nrows * pl.nrows * pl.Ntc);  // pguresvt.hpp:60
     double startp = (p.lambda >= 0.0) ? p.lambda : accu2(C, [&](size_t i) { return u[i]; }) * OoN;
@@ -736,7 +744,7 @@ WindowOut run_window(const double* X, const double* Z, const orc_params& p, cons
     } else {
       sr = batch_search(rf, upper * 1e-4, upper, K, R, p.tol, maxe, true);
     }
-    out = {sr.lambda, sr.risk, sr.evals};
+    out = {sr.lambda, sr.risk, sr.evals, na, nm, ns};
   }
   std::vector<double> v(C);
   pg.svt0.reconstruct(out.lambda, v.data());
@@ -852,6 +860,13 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs, 
   });
 }
 
+int orc_noise_estimate(const double* u, uint32_t nrows, uint32_t ncols, uint32_t nslices,
+                       uint32_t method, double* alpha, double* mu, double* sigma) {
+  return guarded([&] {
+    orc_noise_estimate_impl(u, nrows, ncols, nslices, method, *alpha, *mu, *sigma);
+  });
+}
+
 int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,
                       uint32_t r) {
   return guarded([&] { median_frame(src, dst, (int)nx, (int)ny, (int)r); });
@@ -885,9 +900,9 @@ int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimage
       const WindowOut o = run_window(X, Z.empty() ? nullptr : Z.data(), *p, pl, t,
                                      Y + (size_t)t * F);
       est[t] = o.lambda;  // pguresvt.hpp:150-153 (unswapped alpha, mu, sigma)
-      est[t + nimages] = p->alpha;
-      est[t + 2 * (size_t)nimages] = p->mu;
-      est[t + 3 * (size_t)nimages] = p->sigma;
+      est[t + nimages] = o.alpha;
+      est[t + 2 * (size_t)nimages] = o.mu;
+      est[t + 3 * (size_t)nimages] = o.sigma;
       evals[t] = o.evals;
       if (p->risk_out) p->risk_out[t] = o.risk;
       if (p->evals_out) p->evals_out[t] = o.evals;

@@ -80,6 +80,12 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs,
                     int64_t seed, uint32_t compat, const double* lambdas,
                     uint32_t nl, double* risk);
 
+/* Noise parameters of a normalised window (NoiseEstimator::Estimate,
+ * noise.hpp:36-152): u is nrows x ncols x nslices; alpha/mu/sigma hold the
+ * user values (< 0: estimate) on entry and the results on exit. */
+int orc_noise_estimate(const double* u, uint32_t nrows, uint32_t ncols, uint32_t nslices,
+                       uint32_t method, double* alpha, double* mu, double* sigma);
+
 /* Median of the (2r+1)^2 window with clamped coordinates (the reference's
  * ConstantTimeMedianFilter, medfilter.hpp:478-541); nx is the fast axis. */
 int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,

@@ -276,9 +276,15 @@ void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
     throw Fail(PGSVT_ERR_UNSUPPORTED, "motion_filter (median radius) above 15 in this build");
   if (p.median_size > 0 && 2 * p.median_size + 1 > (int64_t)nr)
     throw Fail(PGSVT_ERR_INVALID_ARG, "motion_filter window wider than the frame");
-  if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0))
-    throw Fail(PGSVT_ERR_UNSUPPORTED,
-               "noise estimation is not built: give noise alpha, mu and sigma (>= 0)");
+  if (p.optimize_pgure && (p.alpha < 0 || p.mu < 0 || p.sigma < 0)) {  // noise estimation
+    if (nr > 8 && (nr & (nr - 1)))
+      throw Fail(PGSVT_ERR_UNSUPPORTED, "noise estimation needs power-of-two frames "
+                                        "(noise.hpp:216 has F-test values for 2^k blocks only); "
+                                        "give alpha, mu and sigma");
+    if (nr < 4) throw Fail(PGSVT_ERR_INVALID_ARG, "noise estimation needs frames of side >= 4");
+    if (p.noise_method != 3 && p.noise_method != 4)
+      throw Fail(PGSVT_ERR_UNSUPPORTED, "noise_method 1 and 2 are not built (3 and 4 are)");
+  }
   if (!p.optimize_pgure && !(p.lambda >= 0))
     throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid lambda1 parameter: must be >= 0 without optimisation");
   if (p.search_points > (uint32_t)kMaxK)
@@ -470,6 +476,33 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   stats.d2h += sizeof(double) * nimg;
   for (double v : hmax)
     if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
+  // noise estimation tables per input frame (noise.cu)
+  const bool estimate = pb.optimize && (p.alpha < 0 || p.mu < 0 || p.sigma < 0);
+  NoiseFrames nf{};
+  if (estimate) {
+    nf.nlev = noise_levels(S);
+    const int B = noise_blocks(nf.nlev);
+    nf.maxNodes = 1 + 8 * B;
+    int lbig = 0;  // levels of side >= 128, whose children can exceed 32
+    for (int sz = S; sz >= 128; sz >>= 1) ++lbig;
+    nf.maxBig = 1 + 8 * noise_blocks(lbig);
+    const size_t nn = (size_t)nimg * nf.maxNodes;
+    nf.split = mem.arr<uint8_t>(std::max<size_t>(1, (size_t)nimg * B));
+    nf.nodes = mem.arr<int4>(nn);
+    nf.isdel = mem.arr<uint8_t>(nn);
+    nf.leaf = mem.arr<int4>(nn);
+    nf.nleaf = mem.arr<int>(nimg);
+    nf.big = mem.arr<int>(nn);
+    nf.nbig = mem.arr<int>(nimg);
+    nf.stats = mem.arr<double>(nn * 3);
+    nf.err = mem.arr<int>(1);
+    PGSVT_CK(cudaMemsetAsync(nf.err, 0, sizeof(int), s));
+    check_launch(launch_noise_frames(xs, x64, nimg, S, nf, s), stats, 6);
+    int herr = 0;
+    PGSVT_CK(cudaMemcpyAsync(&herr, nf.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+    if (herr) throw Fail(PGSVT_ERR_CUDA, "noise estimation: quadtree replay overflow");
+  }
   // median pre-filter of the ARPS input (pguresvt.hpp:69-84)
   float* zs = nullptr;
   double* zmx = nullptr;
@@ -565,6 +598,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } evg{ready};
   PGSVT_CK(cudaEventRecord(ready, s));
 
+  std::vector<NoiseWindows> nws(NS);
   std::vector<Lane> lanes(NS);
   struct LaneGuard {
     std::vector<Lane>& l;
@@ -623,6 +657,15 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
     d.wc = mem.arr<WinConst>(W);
     d.st = mem.arr<SearchState>(W);
+    if (estimate) {
+      NoiseWindows& nw = nws[li];
+      nw.method = (int)p.noise_method;
+      const size_t per = (size_t)g.nwin * nf.maxNodes;
+      nw.mean = mem.arr<double>((size_t)W * per);
+      nw.x = mem.arr<double>((size_t)W * per);
+      nw.y = mem.arr<double>((size_t)W * per);
+      nw.hist = mem.arr<int>((size_t)W * (per + 1));
+    }
     d.model = dmodel;
     d.model_bf16 = dmodel_bf;
     d.feat_slots = fslots;
@@ -673,6 +716,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     }
     clk.mark(7);  // probe uploads and other gaps
     check_launch(launch_window_setup(pbb, d, L.s), stats, 2);
+    if (estimate) check_launch(launch_noise_windows(pbb, d, nf, nws[bi % NS], L.s), stats, 3);
     clk.mark(1);
     check_launch(launch_arps(pbb, d, L.s), stats, pbb.motion ? 2 : 1);
     clk.mark(2);

@@ -563,9 +563,9 @@ __global__ void k_output(Problem pb, DeviceBuffers d) {
     }
     if (d.evals_out) d.evals_out[wc.t] = (uint32_t)d.st[w].evals_total;
     d.est[wc.t] = d.st[w].final_lambda;
-    d.est[wc.t + n] = pb.alpha_c;
-    d.est[wc.t + 2 * (size_t)n] = pb.mu_c;
-    d.est[wc.t + 3 * (size_t)n] = pb.sigma_c;
+    d.est[wc.t + n] = wc.est_alpha;
+    d.est[wc.t + 2 * (size_t)n] = wc.est_mu;
+    d.est[wc.t + 3 * (size_t)n] = wc.est_sigma;
   }
 }
 

@@ -68,6 +68,7 @@ struct WinConst {
                    // window (the reference's 0/0 ends as a zero output frame)
   double sum_u;    // accu(u)
   double alpha, mu, sigma;  // PGURE members (after the argument binding)
+  double est_alpha, est_mu, est_sigma;  // caller-side values (estimates(t, 1..3))
   double eps1, eps2;
   double start, upper;      // lambda search start point / upper bound
   int32_t t;                // output frame index
@@ -203,6 +204,34 @@ cudaError_t launch_cube_out(const Problem& pb, const DeviceBuffers& d, double* v
                             cudaStream_t s);
 cudaError_t launch_risk_round(const Problem& pb, const DeviceBuffers& d, double* out,
                               cudaStream_t s);
+
+// noise estimation (noise.cu): per input frame ...
+struct NoiseFrames {
+  int nlev, maxNodes, maxBig;
+  uint8_t* split;   // [nimg][blocks of side > 8] F-test decisions
+  int4* nodes;      // [nimg][maxNodes] quadtree replay scratch
+  uint8_t* isdel;   // [nimg][maxNodes]
+  int4* leaf;       // [nimg][maxNodes] leaves (row, col, side) in the reference's order
+  int* nleaf;       // [nimg]
+  int* big;         // [nimg][maxNodes] indices of leaves of side > 32
+  int* nbig;        // [nimg]
+  double* stats;    // [nimg][maxNodes][3] (a_lo, a_hi, var), raw scale
+  int* err;         // replay overflow flag
+};
+// ... and per window batch
+struct NoiseWindows {
+  int method;
+  double* mean;     // [W][nwin][maxNodes] robust leaf means (normalised)
+  double* x;        // [W][nwin * maxNodes] fit inputs
+  double* y;
+  int* hist;        // [W][nwin * maxNodes + 1]
+};
+int noise_levels(int S);
+int noise_blocks(int nlev);
+cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, int S,
+                                const NoiseFrames& nf, cudaStream_t s);
+cudaError_t launch_noise_windows(const Problem& pb, const DeviceBuffers& d, const NoiseFrames& nf,
+                                 const NoiseWindows& nw, cudaStream_t s);
 
 // learned lambda proposal (lambda.cu)
 struct LambdaTrain {

@@ -155,6 +155,9 @@ __global__ void k_window_const(Problem pb, DeviceBuffers d) {
     c.out_slice = g.fw;
     c.ref = g.fw;
   }
+  c.est_alpha = pb.alpha_c;  // replaced by noise.cu when estimated
+  c.est_mu = pb.mu_c;
+  c.est_sigma = pb.sigma_c;
   // PGURE(u, p, alpha, sigma, mu, ...) binds to the ctor's (alpha, mu, sigma)
   c.alpha = pb.alpha_c;
   if (pb.compat & 0x1) {

@@ -206,9 +206,12 @@ def test_errors(capi, pkg):
     with pytest.raises(pkg.PgsvtError) as e:
         capi.denoise(Xn, p)
     assert e.value.code == capi.ERR_NONFINITE
-    with pytest.raises(pkg.PgsvtError) as e:
-        capi.denoise(X, capi.default_params(optimize_pgure=0, lambda_=0.1))  # median 5
+    with pytest.raises(pkg.PgsvtError) as e:  # median window 2*16+1 wider than the frame
+        capi.denoise(X, capi.default_params(optimize_pgure=0, lambda_=0.1, median_size=16))
     assert e.value.code == capi.ERR_UNSUPPORTED
+    with pytest.raises(pkg.PgsvtError) as e:  # 2*8+1 > 16
+        capi.denoise(X, capi.default_params(optimize_pgure=0, lambda_=0.1, median_size=8))
+    assert e.value.code == capi.ERR_INVALID_ARG
     with pytest.raises(pkg.PgsvtError) as e:
         capi.denoise(X[:, :, :8], p)  # shorter than the trajectory
     assert e.value.code == capi.ERR_INVALID_ARG

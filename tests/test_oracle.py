@@ -252,19 +252,40 @@ def test_denoise_threads_do_not_change_results(oracle):
 
 @pytest.mark.skipif(not reference_available(), reason="reference test data not mounted")
 def test_reference_fixture_quality_bound(oracle):
-    """The reference's end-to-end fixture (pguresvt/tests/test_svt.py:61-101):
-    N(100, 100^2) noise on data.npz; NSED to the clean data below 0.025.
-    The median pre-filter and noise estimation are not restated, so the
-    noise parameters are given and the filter is off."""
+    """The reference's end-to-end fixture (pguresvt/tests/test_svt.py:61-106):
+    N(100, 100^2) noise on data.npz.  With the SVT defaults (median filter 5,
+    noise parameters estimated, PGURE on) and with a fixed lambda the NSED to
+    the clean data is below 0.025 (test_single_threaded, test_opt_lambda1);
+    with the noise mu and sigma given in counts it is below 0.3
+    (test_known_noise)."""
     X = np.load(os.path.join(REFERENCE, "pguresvt", "tests", "data.npz"))["a"]
     rng = np.random.RandomState(101)
     Y = X + 100.0 + 100.0 * rng.randn(*X.shape)
     Y[Y < 0.0] = 0.0
     Y = Y.astype(np.uint16)
-    for kw in (dict(optimize_pgure=0, lambda_=5.0),
-               dict(optimize_pgure=1, alpha=0.1, mu=100.0, sigma=100.0, random_seed=101)):
-        Yd, _, _ = oracle.denoise(Y, n_jobs=4, median_size=-1, **kw)
-        assert _nsed(X, Yd) < 0.025
+    for kw, bound in ((dict(), 0.025), (dict(lambda_=5.0), 0.025),
+                      (dict(optimize_pgure=0, lambda_=5.0), 0.025),
+                      (dict(mu=100.0, sigma=100.0), 0.3)):
+        Yd, est, _ = oracle.denoise(Y, n_jobs=4, median_size=5, random_seed=101, **kw)
+        assert _nsed(X, Yd) < bound, kw
+        if kw.get("optimize_pgure", 1):
+            assert np.all(est[:, 1:] >= 0)  # estimated alpha, mu, sigma
+
+
+def test_noise_estimator_frozen(oracle):
+    """Frozen outputs of the noise estimator restatement (noise.hpp:36-152)
+    for methods 1-4 on seeded windows (tests/golden/make_noise_golden.py)."""
+    z = np.load(os.path.join(GOLDEN, "noise.npz"))
+    for k in range(int(z["n"])):
+        for method in (1, 2, 3, 4):
+            est = oracle.noise_estimate(z["u_%d" % k], method=method)
+            np.testing.assert_allclose(est, z["est_%d" % k][method - 1], rtol=1e-12)
+
+
+def test_noise_estimator_keeps_given_values(oracle):
+    z = np.load(os.path.join(GOLDEN, "noise.npz"))
+    a, m, s = oracle.noise_estimate(z["u_0"], alpha=0.5, mu=-1, sigma=0.25)
+    assert a == 0.5 and s == 0.25 and m >= 0
 
 
 # ---- median pre-filter (medfilter.hpp:478-541 via pguresvt.hpp:69-80)
