@@ -47,15 +47,19 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--hint", type=float, default=-1.0, help="fixed lambda proposal")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-lambda arm")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also time pgsvt_denoise_batch on this many uneven sequences")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="SVD kernel form: 1 tuned (default), 0 registers, 3 shared memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=0, help="patch stride of the CPU sample")
     return ap.parse_args()
 
 
-def params(capi, a, m, s, bs, hint):
+def params(capi, a, m, s, bs, hint, autotune=1):
     return capi.default_params(traj_length=15, block_size=bs, block_overlap=1, motion_window=7,
                                median_size=-1, random_seed=7, optimize_pgure=1, alpha=a, mu=m,
-                               sigma=s, lambda_hint=hint)
+                               sigma=s, lambda_hint=hint, autotune=autotune)
 
 
 class ClockSampler:
@@ -124,6 +128,58 @@ def psnr(clean, y):
 def svd_flops(m, n):
     """Golub-Van Loan thin-SVD operation count 14mn^2 + 8n^3 per matrix."""
     return 14 * m * n * n + 8 * n ** 3
+
+
+def batch_workload(n, seed):
+    """Sequences of the uneven-batch configuration, scaled to bench time:
+    sides {128, 256, 384, 512}, 30-45 frames, patch {4, 6, 8}, trajectory
+    {9, 15, 21}, alpha U[0.05, 1], sigma U[0.5, 5], the blob generator with
+    sub-pixel drift; 16 fixed lambda values per sequence."""
+    pkg = entry.load_package()
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(rng.choice([128, 256, 384, 512]))
+        nt = int(rng.integers(30, 46))
+        bs = int(rng.choice([4, 6, 8]))
+        T = int(rng.choice([9, 15, 21]))
+        a, sg = float(rng.uniform(0.05, 1.0)), float(rng.uniform(0.5, 5.0))
+        nb = max(1, int(round(80 * (side / 256.0) ** 2)))
+        clean = pkg.synth.blobs(side, nt, nb, seed * 1000 + i, 2.0, False, False)
+        noisy = pkg.synth.poisson_gaussian(clean, a, 0.5, sg, seed * 1000 + i + 1)
+        lam = np.geomspace(1e-3, 100.0, 16) * float(rng.uniform(0.5, 2.0))
+        out.append(dict(X=np.asfortranarray(noisy.astype(np.float32)), bs=bs, T=T,
+                        noise=(a, 0.5, sg), lambdas=lam))
+    return out
+
+
+def run_batch(capi, n, seed, slots=2):
+    seqs = batch_workload(n, seed)
+    inp = []
+    for q in seqs:
+        a, m, s = q["noise"]
+        p = capi.default_params(traj_length=q["T"], block_size=q["bs"], motion_window=7,
+                                median_size=0, random_seed=7, alpha=a, mu=m, sigma=s,
+                                autotune=1)
+        inp.append(dict(X=q["X"], params=p, lambdas=q["lambdas"]))
+    # warm-up: one sequence of every (patch, trajectory) shape, which also runs
+    # the autotuner once per shape outside the timed call
+    first = {}
+    for q, x in zip(seqs, inp):
+        first.setdefault((q["bs"], q["T"]), x)
+    capi.denoise_batch(list(first.values()), slots=slots)
+    t0 = time.perf_counter()
+    res, st = capi.denoise_batch(inp, slots=slots)
+    dt = time.perf_counter() - t0
+    frames = sum(q["X"].shape[2] for q in seqs)
+    vox = sum(q["X"].size for q in seqs)
+    return {"sequences": n, "frames": frames, "voxels": int(vox), "seconds": dt,
+            "value": frames / dt, "unit": "frames/s (e2e, host buffers)", "slots": slots,
+            "risk_evals_per_window": st.risk_evals / max(1, st.windows),
+            "gpu_launches": int(st.kernel_launches),
+            "config": "sides {128,256,384,512}, 30-45 frames, patch {4,6,8}, T {9,15,21}, "
+                      "16 fixed lambda per sequence (uneven-batch configuration scaled to "
+                      "%d sequences)" % n}
 
 
 def cpu_baseline(noisy, nm, bs, evals_per_window, stride, threads, nsample):
@@ -199,7 +255,7 @@ def main():
     noisy, (a, m, s), clean = make_workload(args.side, args.frames, args.seed + rank, True)
     S, nimg = args.side, args.frames
     n = S * S * nimg
-    p = params(capi, a, m, s, args.patch, args.hint)
+    p = params(capi, a, m, s, args.patch, args.hint, args.autotune)
 
     # ---- device-resident timing
     x = torch.from_numpy(np.ascontiguousarray(noisy.ravel(order="F"))).cuda()
@@ -247,7 +303,7 @@ def main():
     learned = None
     if not args.no_learned:
         model = pkg.learned.load_model()
-        pl = params(capi, a, m, s, args.patch, -1.0)
+        pl = params(capi, a, m, s, args.patch, -1.0, args.autotune)
         pl.lambda_model = model.ctypes.data
         step(pl)
         torch.cuda.synchronize()
@@ -352,7 +408,11 @@ def main():
             "risk_evals_per_window": evals_per_window,
             "arps_exact_steps": int(st.arps_exact_steps),
             "svd_fp64_tests": int(st.svd_fp64_tests),
-            "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8)}
+            "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8),
+            "svd_variant": {0: "registers", 1: "more lanes per patch",
+                            2: "shared memory"}.get(int(st.svd_variant), "?")}
+    if args.batch:
+        line["batch"] = run_batch(capi, args.batch, args.seed)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(noisy, (a, m, s), args.patch, evals_per_window,

@@ -114,8 +114,10 @@ typedef struct {
                                window batch of each patch size / window
                                length seen by the process and keep the
                                fastest (results agree to FP32 rounding);
-                               0: the default shape; 2: the alternative
-                               shape where the patch size has one            */
+                               0: the default shape; 2: more lanes per
+                               patch where the patch size has that form;
+                               3: the default shape with its columns in
+                               shared memory                                 */
 } pgsvt_params;
 
 /* Optional per-frame outputs of pgsvt_denoise_ex / pgsvt_denoise_device_ex

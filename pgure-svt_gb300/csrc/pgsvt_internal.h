@@ -266,6 +266,7 @@ int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
 int svd_columns(int nwin);
 int svd_variants(int M);
+bool svd_variant_ok(int M, int v);
 bool svd_supported(int bs, int nwin);
 
 }  // namespace pgsvt

@@ -25,7 +25,7 @@
 
 namespace pgsvt {
 namespace svdk {
-template <int RPL, int LANES, int NC>
+template <int RPL, int LANES, int NC, bool SM>
 cudaError_t run_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 }
 
@@ -41,13 +41,26 @@ bool svd_supported(int bs, int nwin) {
   return bs >= 2 && bs <= 8 && svd_columns(nwin) > 0;
 }
 
-// Kernel shapes: rows per lane x lanes per patch covers bs*bs rows; the
-// instantiations live in svd_i*.cu so that they compile in parallel.
-// Variant 0 is the default shape of each patch size; variant 1 spreads a
-// patch over more lanes (fewer registers per lane, more shuffles per inner
-// product).  Both give the same results up to FP32 rounding; the autotuner
-// (capi.cu) times them on the caller's data and keeps the faster one.
-int svd_variants(int M) { return (M > 16 && M <= 32) ? 1 : 2; }
+// Kernel forms: rows per lane x lanes per patch covers bs*bs rows; the
+// instantiations live in svd_i*.cu / svd_s*.cu so that they compile in
+// parallel.  Variant 0 is the default shape with the columns in registers
+// (moved one position per round), variant 1 spreads a patch over more lanes
+// (fewer registers per lane, more shuffles per inner product), variant 2 is the
+// default shape with the columns in shared memory (addressed by the round's
+// schedule, no moves).  Variants 0 and 2 apply the same rotations in the same
+// order; all agree to FP32 rounding.  The autotuner (capi.cu) times them on the
+// caller's data and keeps the fastest.
+bool svd_variant_ok(int M, int v) {
+  if (v == 0 || v == 2) return true;
+  return v == 1 && !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
+}
+int svd_variants(int M) { return svd_variant_ok(M, 1) ? 3 : 2; }
+
+template <int RPL, int LANES, int NC>
+cudaError_t run_pair(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+  return pb.svd_variant == 2 ? svdk::run_svd<RPL, LANES, NC, true>(pb, d, s)
+                             : svdk::run_svd<RPL, LANES, NC, false>(pb, d, s);
+}
 
 cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   using namespace svdk;
@@ -55,33 +68,33 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
   const bool alt = pb.svd_variant == 1;
   if (M <= 16) {  // bs 2..4
     if (alt) {
-      if (NC == 10) return run_svd<2, 8, 10>(pb, d, s);
-      if (NC == 16) return run_svd<2, 8, 16>(pb, d, s);
+      if (NC == 10) return run_svd<2, 8, 10, false>(pb, d, s);
+      if (NC == 16) return run_svd<2, 8, 16, false>(pb, d, s);
     }
-    if (NC == 10) return run_svd<4, 4, 10>(pb, d, s);
-    if (NC == 16) return run_svd<4, 4, 16>(pb, d, s);
+    if (NC == 10) return run_pair<4, 4, 10>(pb, d, s);
+    if (NC == 16) return run_pair<4, 4, 16>(pb, d, s);
   } else if (M <= 32) {  // bs 5
-    if (NC == 10) return run_svd<4, 8, 10>(pb, d, s);
-    if (NC == 16) return run_svd<4, 8, 16>(pb, d, s);
-    if (NC == 22) return run_svd<4, 8, 22>(pb, d, s);
+    if (NC == 10) return run_pair<4, 8, 10>(pb, d, s);
+    if (NC == 16) return run_pair<4, 8, 16>(pb, d, s);
+    if (NC == 22) return run_pair<4, 8, 22>(pb, d, s);
   } else if (M <= 40) {  // bs 6
     if (alt) {
-      if (NC == 10) return run_svd<3, 16, 10>(pb, d, s);
-      if (NC == 16) return run_svd<3, 16, 16>(pb, d, s);
-      if (NC == 22) return run_svd<3, 16, 22>(pb, d, s);
+      if (NC == 10) return run_svd<3, 16, 10, false>(pb, d, s);
+      if (NC == 16) return run_svd<3, 16, 16, false>(pb, d, s);
+      if (NC == 22) return run_svd<3, 16, 22, false>(pb, d, s);
     }
-    if (NC == 10) return run_svd<5, 8, 10>(pb, d, s);
-    if (NC == 16) return run_svd<5, 8, 16>(pb, d, s);
-    if (NC == 22) return run_svd<5, 8, 22>(pb, d, s);
+    if (NC == 10) return run_pair<5, 8, 10>(pb, d, s);
+    if (NC == 16) return run_pair<5, 8, 16>(pb, d, s);
+    if (NC == 22) return run_pair<5, 8, 22>(pb, d, s);
   } else {  // bs 7, 8
     if (alt) {
-      if (NC == 10) return run_svd<2, 32, 10>(pb, d, s);
-      if (NC == 16) return run_svd<2, 32, 16>(pb, d, s);
-      if (NC == 22) return run_svd<2, 32, 22>(pb, d, s);
+      if (NC == 10) return run_svd<2, 32, 10, false>(pb, d, s);
+      if (NC == 16) return run_svd<2, 32, 16, false>(pb, d, s);
+      if (NC == 22) return run_svd<2, 32, 22, false>(pb, d, s);
     }
-    if (NC == 10) return run_svd<4, 16, 10>(pb, d, s);
-    if (NC == 16) return run_svd<4, 16, 16>(pb, d, s);
-    if (NC == 22) return run_svd<4, 16, 22>(pb, d, s);
+    if (NC == 10) return run_pair<4, 16, 10>(pb, d, s);
+    if (NC == 16) return run_pair<4, 16, 16>(pb, d, s);
+    if (NC == 22) return run_pair<4, 16, 22>(pb, d, s);
   }
   return cudaErrorInvalidValue;
 }

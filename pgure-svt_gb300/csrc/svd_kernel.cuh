@@ -62,6 +62,61 @@ __device__ __forceinline__ bool can_survive(const Problem& pb, float s, float sm
   return 2.f * logf(smax / s) < 1.05f * upper * (s * s) + 1e-6f;
 }
 
+// Rotation of one pair from the half-angle identities: with d = be - al,
+// r = sqrt(d^2 + 4g^2), cos 2th = |d| / r and sin 2th = 2 g sign(d) / r (the
+// smaller of the two orthogonalising angles, sign(0) = +1): cos th =
+// sqrt((1 + cos 2th) / 2), sin th = sin 2th / (2 cos th).  Flags whether the
+// pair was near-degenerate within the FP64 band.
+__device__ __forceinline__ void rotation(float al, float be, float gv, float g2, float ab,
+                                         float& cs, float& sn, bool& definite, bool& band) {
+  const bool degen = fabsf(be - al) <= kDegen * (al + be);
+  if (degen && g2 <= (kBand * kBand * kTol * kTol) * ab) band = true;
+  else definite = true;
+  const float dd = be - al;
+  const float ir = rsqrtf(fmaf(dd, dd, 4.f * g2));
+  const float hh = fmaf(0.5f * fabsf(dd), ir, 0.5f);  // (1 + cos 2th) / 2
+  const float rh = rsqrtf(hh);
+  cs = hh * rh;
+  sn = (dd >= 0.f ? gv : -gv) * ir * rh;
+}
+
+// |c a - s b|^2 and |s a + c b|^2 from al = |a|^2, be = |b|^2, g = a.b
+__device__ __forceinline__ void rotated_norms(float al, float be, float gv, float cs, float sn,
+                                              float& ni, float& nj) {
+  const float c2 = cs * cs, s2 = sn * sn, csg = 2.f * cs * sn * gv;
+  ni = fmaf(c2, al, fmaf(s2, be, -csg));
+  nj = fmaf(s2, al, fmaf(c2, be, csg));
+}
+
+// RPL consecutive floats of one lane (16-byte vectors when RPL % 4 == 0)
+template <int RPL>
+__device__ __forceinline__ void load_rows(const float* p, float (&v)[RPL]) {
+  if constexpr (RPL % 4 == 0) {
+#pragma unroll
+    for (int r = 0; r < RPL; r += 4) {
+      const float4 t = *reinterpret_cast<const float4*>(p + r);
+      v[r] = t.x;
+      v[r + 1] = t.y;
+      v[r + 2] = t.z;
+      v[r + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) v[r] = p[r];
+  }
+}
+template <int RPL>
+__device__ __forceinline__ void store_rows(float* p, const float (&v)[RPL]) {
+  if constexpr (RPL % 4 == 0) {
+#pragma unroll
+    for (int r = 0; r < RPL; r += 4)
+      *reinterpret_cast<float4*>(p + r) = make_float4(v[r], v[r + 1], v[r + 2], v[r + 3]);
+  } else {
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) p[r] = v[r];
+  }
+}
+
 // Rounds unrolled per loop iteration (code size vs register moves of the
 // round shift) and the residency target of the launch bounds.
 #ifndef PGSVT_SVD_UNROLL
@@ -70,13 +125,37 @@ __device__ __forceinline__ bool can_survive(const Problem& pb, float s, float sm
 #ifndef PGSVT_SVD_MINBLOCKS
 #define PGSVT_SVD_MINBLOCKS 3
 #endif
+#ifndef PGSVT_SVD_MINBLOCKS_SM
+#define PGSVT_SVD_MINBLOCKS_SM 4
+#endif
 
-template <int RPL, int LANES, int NC>
-__global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, DeviceBuffers d,
-                                                                  int nitems) {
+// Shared-memory footprint of one patch: SM keeps the columns there during the
+// sweeps ([NC][MP] plus NC norms, the patch stride an odd multiple of 16
+// floats so the two 4-lane patches of a quarter-warp use disjoint banks);
+// otherwise the epilogue's staging copy ([NC][MP+1]).
+template <int RPL, int LANES, int NC, bool SM>
+struct SvdSmem {
+  static constexpr int MP = RPL * LANES;
+  static constexpr int CS = SM ? MP : MP + 1;  // column stride
+  static constexpr int NRM = ((NC + 15) / 16) * 16;
+  static constexpr int BASE = NC * MP + NRM;
+  static constexpr int STRIDE = SM ? ((LANES == 4 && BASE % 32 == 0) ? BASE + 16 : BASE)
+                                   : NC * (MP + 1) + 4;
+};
+
+// residency target: the shared-memory form holds a round's column pairs in
+// registers, (NC/2) * 2 * RPL floats
+template <int RPL, int NC, bool SM>
+constexpr int svd_minblocks() {
+  return SM ? ((NC / 2) * 2 * RPL <= 64 ? PGSVT_SVD_MINBLOCKS_SM : 2) : PGSVT_SVD_MINBLOCKS;
+}
+
+template <int RPL, int LANES, int NC, bool SM = false>
+__global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
+    k_svd(Problem pb, DeviceBuffers d, int nitems) {
   constexpr int GROUPS = 32 / LANES;
-  constexpr int MP = RPL * LANES;               // padded rows
-  constexpr int GSTRIDE = NC * (MP + 1) + 4;    // smem floats per patch
+  constexpr int GSTRIDE = SvdSmem<RPL, LANES, NC, SM>::STRIDE;  // smem floats per patch
+  constexpr int CS = SvdSmem<RPL, LANES, NC, SM>::CS;
   constexpr int U = ((NC - 1) % PGSVT_SVD_UNROLL == 0) ? PGSVT_SVD_UNROLL : 1;
   const Geometry& g = pb.g;
   const int lane = threadIdx.x & 31;
@@ -125,6 +204,9 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
     return v;
   };
 
+  extern __shared__ float smem[];
+  float* As = smem + (size_t)(wib * GROUPS + grp) * GSTRIDE;  // [NC][CS]
+
   // ---- gather B (svt.hpp:101-109)
   float A[RPL][NC];
 #pragma unroll
@@ -136,93 +218,27 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
       base = (size_t)k * F + (pc & 0xffffu) + (size_t)(pc >> 16) * g.S;
     }
 #pragma unroll
-    for (int r = 0; r < RPL; ++r) A[r][k] = (colok && roff[r] >= 0) ? value(base + roff[r]) : 0.f;
+    for (int r = 0; r < RPL; ++r) {
+      const float v = (colok && roff[r] >= 0) ? value(base + roff[r]) : 0.f;
+      if constexpr (SM) As[k * CS + q * RPL + r] = v;
+      else A[r][k] = v;
+    }
   }
 
-  extern __shared__ float smem[];
-  float* As = smem + (size_t)(wib * GROUPS + grp) * GSTRIDE;  // [NC][MP+1]
-
   // ---- Jacobi sweeps
-  float nrm[NC];
   int sweeps = 0;
   unsigned fp64_tests = 0;
-#pragma unroll 1
-  for (; sweeps < kMaxSweeps; ++sweeps) {
-#pragma unroll
-    for (int k = 0; k < NC - 1; ++k) {
-      float s = 0.f;
-#pragma unroll
-      for (int r = 0; r < RPL; ++r) s = fmaf(A[r][k], A[r][k], s);
-      nrm[k] = lanes_sum<LANES>(s);
-    }
-    nrm[NC - 1] = 0.f;
-    bool definite = false, band = false;
-#pragma unroll U
-    for (int rd = 0; rd < NC - 1; ++rd) {
-      float gm[NC / 2];
-#pragma unroll
-      for (int pp = 1; pp < NC / 2; ++pp) {
-        float s = 0.f;
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) s = fmaf(A[r][pp], A[r][NC - 1 - pp], s);
-        gm[pp] = s;
-      }
-#pragma unroll
-      for (int o = 1; o < LANES; o <<= 1)
-#pragma unroll
-        for (int pp = 1; pp < NC / 2; ++pp) gm[pp] += __shfl_xor_sync(0xffffffffu, gm[pp], o);
-#pragma unroll
-      for (int pp = 1; pp < NC / 2; ++pp) {
-        const int pi = pp, pj = NC - 1 - pp;
-        const float al = nrm[pi], be = nrm[pj], gv = gm[pp];
-        const float g2 = gv * gv, ab = al * be;
-        const bool need = g2 > (kTol * kTol) * ab;
-        if (!__any_sync(0xffffffffu, need)) continue;  // converged pair in every lane
-        if (need) {
-          const bool degen = fabsf(be - al) <= kDegen * (al + be);
-          if (degen && g2 <= (kBand * kBand * kTol * kTol) * ab) band = true;
-          else definite = true;
-          // Rotation angle from the half-angle identities: with d = be - al,
-          // r = sqrt(d^2 + 4g^2), cos 2th = |d| / r and sin 2th = 2 g sign(d) / r
-          // (the smaller of the two orthogonalising angles, sign(0) = +1):
-          // cos th = sqrt((1 + cos 2th) / 2), sin th = sin 2th / (2 cos th).
-          const float dd = be - al;
-          const float ir = rsqrtf(fmaf(dd, dd, 4.f * g2));
-          const float hh = fmaf(0.5f * fabsf(dd), ir, 0.5f);  // (1 + cos 2th) / 2
-          const float rh = rsqrtf(hh);
-          const float cs = hh * rh;
-          const float sn = (dd >= 0.f ? gv : -gv) * ir * rh;
-#pragma unroll
-          for (int r = 0; r < RPL; ++r) {
-            const float a = A[r][pi], b = A[r][pj];
-            A[r][pi] = fmaf(cs, a, -sn * b);
-            A[r][pj] = fmaf(sn, a, cs * b);
-          }
-          // |c a - s b|^2 and |s a + c b|^2 from al, be, g
-          const float c2 = cs * cs, s2 = sn * sn, csg = 2.f * cs * sn * gv;
-          nrm[pi] = fmaf(c2, al, fmaf(s2, be, -csg));
-          nrm[pj] = fmaf(s2, al, fmaf(c2, be, csg));
-        }
-      }
-      shift_round<RPL, NC>(A, nrm);
-    }
-    if (__any_sync(0xffffffffu, definite)) continue;
-    if (!__any_sync(0xffffffffu, band)) break;
-    // Only near-degenerate pairs moved, by amounts at the FP32 noise level of
-    // their inner products: decide convergence from FP64 inner products of
-    // the current columns (exact products of the FP32 entries).
-#pragma unroll
-    for (int k = 0; k < NC; ++k)
-#pragma unroll
-      for (int r = 0; r < RPL; ++r) As[k * (MP + 1) + q * RPL + r] = A[r][k];
-    __syncwarp();
+  // Only near-degenerate pairs moved, by amounts at the FP32 noise level of
+  // their inner products: decide convergence from FP64 inner products of the
+  // current columns (exact products of the FP32 entries) staged in As.
+  auto fp64_again = [&]() {
     bool again = false;
     for (int i = 0; i < nwin; ++i) {
       for (int j = i + 1; j < nwin; ++j) {
         float gi = 0.f, ai = 0.f, aj = 0.f;
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
-          const float x = As[i * (MP + 1) + q * RPL + r], y = As[j * (MP + 1) + q * RPL + r];
+          const float x = As[i * CS + q * RPL + r], y = As[j * CS + q * RPL + r];
           gi = fmaf(x, y, gi);
           ai = fmaf(x, x, ai);
           aj = fmaf(y, y, aj);
@@ -236,7 +252,7 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
           double g64 = 0.0;
 #pragma unroll
           for (int r = 0; r < RPL; ++r)
-            g64 = fma((double)As[i * (MP + 1) + q * RPL + r], (double)As[j * (MP + 1) + q * RPL + r], g64);
+            g64 = fma((double)As[i * CS + q * RPL + r], (double)As[j * CS + q * RPL + r], g64);
           g64 = lanes_sum_d<LANES>(g64);
           if (cand) {
             ++fp64_tests;
@@ -246,7 +262,140 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
       }
     }
     __syncwarp();
-    if (!__any_sync(0xffffffffu, again)) break;
+    return __any_sync(0xffffffffu, again);
+  };
+  if constexpr (!SM) {
+    // columns in registers; the round-robin moves them one position per round
+    float nrm[NC];
+#pragma unroll 1
+    for (; sweeps < kMaxSweeps; ++sweeps) {
+#pragma unroll
+      for (int k = 0; k < NC - 1; ++k) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) s = fmaf(A[r][k], A[r][k], s);
+        nrm[k] = lanes_sum<LANES>(s);
+      }
+      nrm[NC - 1] = 0.f;
+      bool definite = false, band = false;
+#pragma unroll U
+      for (int rd = 0; rd < NC - 1; ++rd) {
+        float gm[NC / 2];
+#pragma unroll
+        for (int pp = 1; pp < NC / 2; ++pp) {
+          float s = 0.f;
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) s = fmaf(A[r][pp], A[r][NC - 1 - pp], s);
+          gm[pp] = s;
+        }
+#pragma unroll
+        for (int o = 1; o < LANES; o <<= 1)
+#pragma unroll
+          for (int pp = 1; pp < NC / 2; ++pp) gm[pp] += __shfl_xor_sync(0xffffffffu, gm[pp], o);
+#pragma unroll
+        for (int pp = 1; pp < NC / 2; ++pp) {
+          const int pi = pp, pj = NC - 1 - pp;
+          const float al = nrm[pi], be = nrm[pj], gv = gm[pp];
+          const float g2 = gv * gv, ab = al * be;
+          const bool need = g2 > (kTol * kTol) * ab;
+          if (!__any_sync(0xffffffffu, need)) continue;  // converged pair in every lane
+          if (need) {
+            float cs, sn;
+            rotation(al, be, gv, g2, ab, cs, sn, definite, band);
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) {
+              const float a = A[r][pi], b = A[r][pj];
+              A[r][pi] = fmaf(cs, a, -sn * b);
+              A[r][pj] = fmaf(sn, a, cs * b);
+            }
+            rotated_norms(al, be, gv, cs, sn, nrm[pi], nrm[pj]);
+          }
+        }
+        shift_round<RPL, NC>(A, nrm);
+      }
+      if (__any_sync(0xffffffffu, definite)) continue;
+      if (!__any_sync(0xffffffffu, band)) break;
+#pragma unroll
+      for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) As[k * CS + q * RPL + r] = A[r][k];
+      __syncwarp();
+      if (!fp64_again()) break;
+    }
+  } else {
+    // columns in shared memory, addressed by the same round-robin schedule
+    // (position k of round rd holds column (k + rd) mod (NC-1)): the same
+    // rotations in the same order, without moving data
+    float* nrs = As + NC * CS;  // column norms
+#pragma unroll 1
+    for (; sweeps < kMaxSweeps; ++sweeps) {
+#pragma unroll
+      for (int k = 0; k < NC - 1; ++k) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+          const float x = As[k * CS + q * RPL + r];
+          s = fmaf(x, x, s);
+        }
+        s = lanes_sum<LANES>(s);
+        if (q == 0) nrs[k] = s;
+      }
+      if (q == 0) nrs[NC - 1] = 0.f;
+      __syncwarp();
+      bool definite = false, band = false;
+#pragma unroll 1
+      for (int rd = 0; rd < NC - 1; ++rd) {
+        float va[NC / 2][RPL], vb[NC / 2][RPL], gm[NC / 2];
+        int ca[NC / 2], cb[NC / 2];
+#pragma unroll
+        for (int pp = 1; pp < NC / 2; ++pp) {
+          int ia = pp + rd, ib = NC - 1 - pp + rd;
+          if (ia >= NC - 1) ia -= NC - 1;
+          if (ib >= NC - 1) ib -= NC - 1;
+          ca[pp] = ia;
+          cb[pp] = ib;
+          load_rows<RPL>(As + ia * CS + q * RPL, va[pp]);
+          load_rows<RPL>(As + ib * CS + q * RPL, vb[pp]);
+          float s = 0.f;
+#pragma unroll
+          for (int r = 0; r < RPL; ++r) s = fmaf(va[pp][r], vb[pp][r], s);
+          gm[pp] = s;
+        }
+#pragma unroll
+        for (int o = 1; o < LANES; o <<= 1)
+#pragma unroll
+          for (int pp = 1; pp < NC / 2; ++pp) gm[pp] += __shfl_xor_sync(0xffffffffu, gm[pp], o);
+#pragma unroll
+        for (int pp = 1; pp < NC / 2; ++pp) {
+          const float al = nrs[ca[pp]], be = nrs[cb[pp]], gv = gm[pp];
+          const float g2 = gv * gv, ab = al * be;
+          const bool need = g2 > (kTol * kTol) * ab;
+          if (!__any_sync(0xffffffffu, need)) continue;
+          if (need) {
+            float cs, sn;
+            rotation(al, be, gv, g2, ab, cs, sn, definite, band);
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) {
+              const float a = va[pp][r], b = vb[pp][r];
+              va[pp][r] = fmaf(cs, a, -sn * b);
+              vb[pp][r] = fmaf(sn, a, cs * b);
+            }
+            store_rows<RPL>(As + ca[pp] * CS + q * RPL, va[pp]);
+            store_rows<RPL>(As + cb[pp] * CS + q * RPL, vb[pp]);
+            float ni, nj;
+            rotated_norms(al, be, gv, cs, sn, ni, nj);
+            if (q == 0) {
+              nrs[ca[pp]] = ni;
+              nrs[cb[pp]] = nj;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      if (__any_sync(0xffffffffu, definite)) continue;
+      if (!__any_sync(0xffffffffu, band)) break;
+      if (!fp64_again()) break;
+    }
   }
   if (lane == 0) atomicAdd(d.counters + 1, (unsigned long long)(sweeps + 1));
   if (q == 0 && fp64_tests) atomicAdd(d.counters + 2, (unsigned long long)fp64_tests);
@@ -259,8 +408,13 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
     float s = 0.f;
 #pragma unroll
     for (int r = 0; r < RPL; ++r) {
-      s = fmaf(A[r][k], A[r][k], s);
-      As[k * (MP + 1) + q * RPL + r] = A[r][k];
+      if constexpr (SM) {
+        const float x = As[k * CS + q * RPL + r];
+        s = fmaf(x, x, s);
+      } else {
+        s = fmaf(A[r][k], A[r][k], s);
+        As[k * CS + q * RPL + r] = A[r][k];
+      }
     }
     sv[k] = sqrtf(lanes_sum<LANES>(s));
   }
@@ -323,7 +477,7 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
     const float inv = st > 0.f ? 1.f / st : 0.f;
     float a[RPL];
 #pragma unroll
-    for (int r = 0; r < RPL; ++r) a[r] = As[ct * (MP + 1) + q * RPL + r] * inv;  // u_t rows
+    for (int r = 0; r < RPL; ++r) a[r] = As[ct * CS + q * RPL + r] * inv;  // u_t rows
     if (c == 0 && live && use) {
 #pragma unroll
       for (int r = 0; r < RPL; ++r)
@@ -357,26 +511,27 @@ __global__ void __launch_bounds__(128, PGSVT_SVD_MINBLOCKS) k_svd(Problem pb, De
   }
 }
 
-template <int RPL, int LANES, int NC>
+template <int RPL, int LANES, int NC, bool SM>
 cudaError_t run_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
-  constexpr int GROUPS = 32 / LANES, MP = RPL * LANES;
-  constexpr int GSTRIDE = NC * (MP + 1) + 4;
+  constexpr int GROUPS = 32 / LANES;
+  constexpr int GSTRIDE = SvdSmem<RPL, LANES, NC, SM>::STRIDE;
   const int nitems = pb.W * d.ncopies * pb.g.NP;
   const int warps = (nitems + GROUPS - 1) / GROUPS;
   const int wpb = 4;
   const size_t shm = (size_t)wpb * GROUPS * GSTRIDE * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(k_svd<RPL, LANES, NC>,
+  cudaError_t e = cudaFuncSetAttribute(k_svd<RPL, LANES, NC, SM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (e != cudaSuccess) return e;
-  k_svd<RPL, LANES, NC><<<(warps + wpb - 1) / wpb, wpb * 32, shm, s>>>(pb, d, nitems);
+  k_svd<RPL, LANES, NC, SM><<<(warps + wpb - 1) / wpb, wpb * 32, shm, s>>>(pb, d, nitems);
   return cudaGetLastError();
 }
 
 }  // namespace svdk
 }  // namespace pgsvt
 
-#define PGSVT_INSTANTIATE_SVD(RPL, LANES, NC) \
-  template cudaError_t pgsvt::svdk::run_svd<RPL, LANES, NC>(const pgsvt::Problem&, \
-                                                          const pgsvt::DeviceBuffers&, cudaStream_t);
+#define PGSVT_INSTANTIATE_SVD_SM(RPL, LANES, NC, SM)                               \
+  template cudaError_t pgsvt::svdk::run_svd<RPL, LANES, NC, SM>(                    \
+      const pgsvt::Problem&, const pgsvt::DeviceBuffers&, cudaStream_t);
+#define PGSVT_INSTANTIATE_SVD(RPL, LANES, NC) PGSVT_INSTANTIATE_SVD_SM(RPL, LANES, NC, false)
 
 #endif

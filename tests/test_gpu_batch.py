@@ -87,6 +87,22 @@ def test_alternative_svd_shape_matches_oracle(capi, pkg, oracle, bs, T):
     for Y in (Y0, Y1):
         assert np.abs(Y[:, :, f] - Yo[:, :, f]).max() <= 1e-4 * scale
     assert np.abs(Y1[:, :, f] - Y0[:, :, f]).max() <= 1e-4 * scale
+    # the shared-memory form applies the register form's rotations in the same
+    # order: identical results
+    Y2, _, st2 = capi.denoise(X, capi.default_params(autotune=3, **base))
+    assert st2.svd_variant == 2
+    np.testing.assert_array_equal(Y2[:, :, f], Y0[:, :, f])
+
+
+def test_shared_memory_svd_form_with_pgure(capi, pkg):
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=8, side=48, nt=18)
+    base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, frame_begin=6, frame_end=10)
+    Y0, e0, st0 = capi.denoise(noisy, capi.default_params(autotune=0, **base))
+    Y2, e2, st2 = capi.denoise(noisy, capi.default_params(autotune=3, **base))
+    assert st2.svd_variant == 2
+    np.testing.assert_array_equal(Y0, Y2)
+    np.testing.assert_array_equal(e0, e2)
+    assert st0.svd_warp_sweeps == st2.svd_warp_sweeps
 
 
 def test_autotuner_picks_and_caches(capi, pkg):
