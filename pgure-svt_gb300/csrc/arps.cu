@@ -18,6 +18,7 @@ namespace {
 
 
 struct ArpsCtx {
+  bool integer;       // integer-valued input below 2^19: exact integer costs
   const float* fa1;   // normalised window slice a1
   const float* fa2;   // normalised window slice a2
   const float* xa1;   // input frames (exact f32 values) for the FP64 path
@@ -31,13 +32,58 @@ struct ArpsCtx {
 
 template <int BS>
 struct Block {
-  float ref[BS * BS];
+  float ref[BS * BS];  // normalised values, or the raw integers in integer mode
 
   __device__ void load(const ArpsCtx& c, int i, int j) {
+    const float* src = c.integer ? c.xa1 : c.fa1;
 #pragma unroll
     for (int cc = 0; cc < BS; ++cc)
 #pragma unroll
-      for (int r = 0; r < BS; ++r) ref[r + cc * BS] = __ldg(c.fa1 + (i + r) + (size_t)(j + cc) * c.S);
+      for (int r = 0; r < BS; ++r) ref[r + cc * BS] = __ldg(src + (i + r) + (size_t)(j + cc) * c.S);
+  }
+
+  // Integer mode: the exact sum of squared differences D.  The reference's
+  // FP64 cost is D / (umax^2 m) up to an absolute error below
+  // (m + 7) 2^-53 (values <= 1 after normalisation), while two different D
+  // differ by at least 1 / (umax^2 m) > 2 (m + 7) 2^-53 for umax <= 2^19 and
+  // m <= 64: comparing D decides exactly as the reference does, except for
+  // equal D.
+  __device__ double ssd(const ArpsCtx& c, int y, int x) const {
+    unsigned long long acc = 0ull;
+#pragma unroll
+    for (int cc = 0; cc < BS; ++cc)
+#pragma unroll
+      for (int r = 0; r < BS; ++r) {
+        const int a = (int)ref[r + cc * BS];
+        const int b = (int)__ldg(c.xa2 + (y + r) + (size_t)(x + cc) * c.S);
+        const long long d = a - b;
+        acc += (unsigned long long)(d * d);
+      }
+    return (double)acc;  // < 2^53: exact
+  }
+
+  // the candidate block at (y, x) equals the one at (y2, x2), element by element
+  __device__ bool same(const ArpsCtx& c, int y, int x, int y2, int x2) const {
+    bool eq = true;
+#pragma unroll
+    for (int cc = 0; cc < BS; ++cc)
+#pragma unroll
+      for (int r = 0; r < BS; ++r)
+        eq &= __ldg(c.xa2 + (y + r) + (size_t)(x + cc) * c.S) ==
+              __ldg(c.xa2 + (y2 + r) + (size_t)(x2 + cc) * c.S);
+    return eq;
+  }
+
+  // cost of the candidate at (y, x): FP32 with an error bound, or exact D
+  __device__ void cost(const ArpsCtx& c, int y, int x, float& cf, float& err, double& cd) const {
+    if (c.integer) {
+      cd = ssd(c, y, x);
+      cf = 0.f;
+      err = 0.f;
+    } else {
+      cost32(c, y, x, cf, err);
+      cd = 0.0;
+    }
   }
 
   // FP32 cost and a bound on |cost32 - cost64|:
@@ -82,6 +128,41 @@ __device__ double cost64(const ArpsCtx& c, int i, int j, int y, int x) {
     else v1 = __dadd_rn(v1, sq);
   }
   return __dmul_rn(__dadd_rn(v1, v2), oo);
+}
+
+// Integer mode: first index of the least D; equal D decided as the
+// reference does: identical candidate blocks have identical FP64 costs (the
+// first one wins), otherwise the FP64 costs of the tied candidates decide.
+template <int BS>
+__device__ int pick_int(const ArpsCtx& c, const Block<BS>& blk, const double* cd, const bool* ev,
+                        const int (*off)[2], int nslot, int i, int j, int y, int x,
+                        unsigned long long* nexact) {
+  int ks = 2;
+  double best = cd[2];
+  for (int k = 0; k < nslot; ++k)
+    if (ev[k] && (cd[k] < best || (cd[k] == best && k < ks))) {
+      best = cd[k];
+      ks = k;
+    }
+  bool tie = false, distinct = false;
+  for (int k = 0; k < nslot; ++k) {
+    if (!ev[k] || k == ks || cd[k] != best) continue;
+    tie = true;
+    if (!blk.same(c, y + off[k][1], x + off[k][0], y + off[ks][1], x + off[ks][0])) distinct = true;
+  }
+  if (!tie || !distinct) return ks;
+  atomicAdd(nexact, 1ull);
+  int kb = -1;
+  double m = 0.0;
+  for (int k = 0; k < nslot; ++k) {
+    if (!ev[k] || cd[k] != best) continue;
+    const double v = cost64<BS>(c, i, j, y + off[k][1], x + off[k][0]);
+    if (kb < 0 || v < m) {
+      m = v;
+      kb = k;
+    }
+  }
+  return kb;
 }
 
 // First index of the minimum among evaluated slots; recomputes in FP64 when
@@ -140,9 +221,15 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
   };
   int x = j, y = i;
   float cs[6], es[6];
+  double cd[6];
   bool ev[6];
   float curC, curE;
-  blk.cost32(c, i, j, curC, curE);
+  double curD;
+  blk.cost(c, i, j, curC, curE, curD);
+  auto choose = [&](const int (*off)[2], int nslot) {
+    return c.integer ? pick_int<BS>(c, blk, cd, ev, off, nslot, i, j, y, x, nexact)
+                     : pick<BS>(c, cs, es, ev, off, nslot, i, j, y, x, nexact);
+  };
   mark(0, 0);
   int step, nld;
   int LD[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
@@ -169,19 +256,21 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
   ev[2] = true;
   cs[2] = curC;
   es[2] = curE;
+  cd[2] = curD;
   for (int k = 0; k < nld; ++k) {
     if (k == 2 || step == 0) continue;
     const int vy = y + LD[k][1], hx = x + LD[k][0];
     if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
-    blk.cost32(c, vy, hx, cs[k], es[k]);
+    blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
     ev[k] = true;
     mark(LD[k][1], LD[k][0]);
   }
-  int ks = pick<BS>(c, cs, es, ev, LD, 6, i, j, y, x, nexact);
+  int ks = choose(LD, 6);
   x += LD[ks][0];
   y += LD[ks][1];
   curC = cs[ks];
   curE = es[ks];
+  curD = cd[ks];
   // SDSP (arps.hpp:299-368); every move enters an unvisited cell, so the loop
   // ends within Wd*Wd iterations.
   const int SD[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
@@ -190,22 +279,24 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
     ev[2] = true;
     cs[2] = curC;
     es[2] = curE;
+    cd[2] = curD;
     for (int k = 0; k < 5; ++k) {
       if (k == 2) continue;
       const int vy = y + SD[k][1], hx = x + SD[k][0];
       if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
       if (hx < j - M || hx > j + M || vy < i - M || vy > i + M) continue;
       if (is_seen(vy - i, hx - j)) continue;
-      blk.cost32(c, vy, hx, cs[k], es[k]);
+      blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
       ev[k] = true;
       mark(vy - i, hx - j);
     }
-    ks = pick<BS>(c, cs, es, ev, SD, 5, i, j, y, x, nexact);
+    ks = choose(SD, 5);
     if (ks == 2) break;
     x += SD[ks][0];
     y += SD[ks][1];
     curC = cs[ks];
     curE = es[ks];
+    curD = cd[ks];
   }
   my = y - i;
   mx = x - j;
@@ -230,6 +321,7 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
   const float* xw = med ? d.zs : d.xs;
   const double* xd = med ? nullptr : d.x64;
   ArpsCtx c;
+  c.integer = med || d.int_input;
   c.umax = med ? wc.wnorm : wc.unorm;
   c.S = g.S;
   c.mw = g.mw;

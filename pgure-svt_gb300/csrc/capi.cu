@@ -470,12 +470,17 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   StageClock clk0(s);
   clk0.mark(0);
   check_launch(launch_convert(X_dev, dtype, (size_t)nimg * F, xs, x64, s), stats);
-  check_launch(launch_frame_max(xs, x64, nimg, F, fmx, s), stats);
+  int* fint = mem.arr<int>(nimg);
+  check_launch(launch_frame_max(xs, x64, nimg, F, fmx, s, fint), stats);
   clk0.mark(0);
   std::vector<double> hmax(nimg);
+  std::vector<int> hint(nimg);
   PGSVT_CK(cudaMemcpyAsync(hmax.data(), fmx, sizeof(double) * nimg, cudaMemcpyDeviceToHost, s));
+  PGSVT_CK(cudaMemcpyAsync(hint.data(), fint, sizeof(int) * nimg, cudaMemcpyDeviceToHost, s));
   PGSVT_CK(cudaStreamSynchronize(s));
-  stats.d2h += sizeof(double) * nimg;
+  stats.d2h += (sizeof(double) + sizeof(int)) * nimg;
+  int int_input = 1;  // ARPS integer mode for integer-valued inputs
+  for (int v : hint) int_input &= v;
   for (double v : hmax)
     if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
   // noise estimation tables per input frame (noise.cu)
@@ -497,6 +502,8 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     nf.big = mem.arr<int>(nn);
     nf.nbig = mem.arr<int>(nimg);
     nf.stats = mem.arr<double>(nn * 3);
+    nf.dup = mem.arr<int>(nn);
+    nf.first = mem.arr<int>((size_t)nimg * noise_blocks(nf.nlev + 1));
     nf.err = mem.arr<int>(1);
     PGSVT_CK(cudaMemsetAsync(nf.err, 0, sizeof(int), s));
     check_launch(launch_noise_frames(xs, x64, nimg, S, nf, s), stats, 6);
@@ -627,6 +634,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.fmax = fmx;
     d.zs = zs;
     d.zmax = zmx;
+    d.int_input = int_input;
     if (zs) d.wz = mem.arr<float>((size_t)W * C);
     d.plist = plist;
     d.counters = counters;
@@ -666,6 +674,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
       nw.mean = mem.arr<double>((size_t)W * per);
       nw.x = mem.arr<double>((size_t)W * per);
       nw.y = mem.arr<double>((size_t)W * per);
+      nw.key = mem.arr<unsigned long long>((size_t)W * per);
       nw.hist = mem.arr<int>((size_t)W * (per + 1));
     }
     d.model = dmodel;

@@ -23,10 +23,16 @@
 //                   stays a leaf), and lists the leaves in its order
 //   k_leaf_stats    one CTA per (frame, leaf): order statistics by 8-bit
 //                   radix selection (IQD bounds, Laplacian median and MAD)
-//   k_leaf_mean     one warp per (window, slice, leaf of side <= 32), one CTA
-//                   per larger leaf: the IRLS robust mean
-//   k_noise_fit     one CTA per window: the IRLS fit, mu, sigma
+//   k_leaf_mean     one warp per (window, slice, leaf of side <= 32, values
+//                   staged in shared memory), one CTA per larger leaf: the
+//                   IRLS robust mean; the recursion lists most blocks twice,
+//                   and every repeated block reuses the first one's results
+//   k_noise_fit     one cluster of 8 CTAs per window (distributed shared
+//                   memory for the sums and the radix selections): the IRLS
+//                   fit, mu, sigma
 // All arithmetic is FP64.
+#include <cooperative_groups.h>
+
 #include "pgsvt.h"
 #include "pgsvt_internal.h"
 
@@ -90,6 +96,17 @@ __device__ double block_sum(double v, double* red) {
   __syncthreads();
   double t = 0.0;
   for (int q = 0; q < nw; ++q) t += red[q];
+  return t;
+}
+
+__device__ double block_max(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[wid] = v;
+  __syncthreads();
+  double t = red[0];
+  for (int q = 1; q < nw; ++q) t = fmax(t, red[q]);
   return t;
 }
 
@@ -181,7 +198,8 @@ __global__ void __launch_bounds__(256) k_quad_decide_small(FrameSrc src, int nle
 // QuadTree (noise.hpp:411-453) replayed over the decision table; writes the
 // leaves (row, col, side) in the reference's order.
 __global__ void k_quad_tree(const uint8_t* split, int nimg, int S, int nlev, int maxNodes,
-                            int4* nodes, uint8_t* isdel, int4* leaf, int* nleaf, int* err) {
+                            int4* nodes, uint8_t* isdel, int4* leaf, int* nleaf, int* dup,
+                            int* first, int* err) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nimg) return;
   const uint8_t* sp = split + (size_t)f * level_off(nlev);
@@ -223,9 +241,20 @@ __global__ void k_quad_tree(const uint8_t* split, int nimg, int S, int nlev, int
     }
     try_split(stk_it[t]++);
   }
+  // leaves in node order; the recursion lists most blocks twice, and a
+  // repeated block (same row, column, side) reuses the first one's statistics
+  int* fi = first + (size_t)f * level_off(nlev + 1);
+  for (int b = 0; b < level_off(nlev + 1); ++b) fi[b] = -1;
   int nl = 0;
-  for (int k = 0; k < len; ++k)
-    if (!dl[k] || k == minDel) leaf[(size_t)f * maxNodes + nl++] = nd[k];
+  for (int k = 0; k < len; ++k) {
+    if (dl[k] && k != minDel) continue;
+    const int4 q = nd[k];
+    const int l = 31 - __clz(S / q.z);
+    const int id = level_off(l) + q.x / q.z + (q.y / q.z) * (1 << l);
+    dup[(size_t)f * maxNodes + nl] = fi[id];
+    if (fi[id] < 0) fi[id] = nl;
+    leaf[(size_t)f * maxNodes + nl++] = q;
+  }
   nleaf[f] = bad ? 0 : nl;
   if (bad) atomicExch(err, 1);
 }
@@ -274,12 +303,12 @@ __device__ void warp_sort(unsigned long long* buf, int n2) {
 // variance of the Laplacian (raw scale): stats = (a_lo, a_hi, var).  One warp
 // per leaf, three sorts of at most 1024 keys in shared memory.
 __global__ void __launch_bounds__(128) k_leaf_stats_small(FrameSrc src, const int4* leaf,
-                                                          const int* nleaf, int maxNodes,
-                                                          double* stats) {
+                                                          const int* nleaf, const int* dup,
+                                                          int maxNodes, double* stats) {
   __shared__ unsigned long long sbuf[4][1024];
   const int f = blockIdx.y, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int li = blockIdx.x * 4 + wib;
-  if (li >= nleaf[f]) return;
+  if (li >= nleaf[f] || dup[(size_t)f * maxNodes + li] >= 0) return;
   const int4 q = leaf[(size_t)f * maxNodes + li];
   if (q.z > 32) return;  // k_leaf_stats_big
   const int N = q.z, n = N * N;
@@ -321,10 +350,12 @@ __global__ void __launch_bounds__(128) k_leaf_stats_small(FrameSrc src, const in
 // The same for leaves of side > 32: one CTA per leaf, radix selection.
 __global__ void __launch_bounds__(256) k_leaf_stats_big(FrameSrc src, const int4* leaf,
                                                         const int* big, const int* nbig,
-                                                        int maxNodes, double* stats) {
+                                                        const int* dup, int maxNodes,
+                                                        double* stats) {
   const int f = blockIdx.y;
   if ((int)blockIdx.x >= nbig[f]) return;
   const int li = big[(size_t)f * maxNodes + blockIdx.x];
+  if (dup[(size_t)f * maxNodes + li] >= 0) return;
   const int4 q = leaf[(size_t)f * maxNodes + li];
   const int N = q.z, n = N * N;
   __shared__ unsigned hist[256];
@@ -357,66 +388,66 @@ struct MeanArgs {
   FrameSrc src;
   const int4* leaf;
   const int* nleaf;
+  const int* dup;
   const double* stats;
   int maxNodes, nwin;
   double* mean;  // [W][nwin][maxNodes]
 };
 
-// RobustMeanEstimate (noise.hpp:239-270) of one leaf of window w, slice k;
-// the weights of an iteration come from the previous (m, 1/d), so nothing is
-// stored per element.  `lanes` threads cooperate (a warp or a block).
-template <bool BLOCK>
-__device__ double robust_mean(const MeanArgs& a, const WinConst& wc, int k, int li, double* red) {
-  const size_t f = (size_t)(wc.s0 + k);
-  const int4 q = a.leaf[f * a.maxNodes + li];
-  const int N = q.z, n = N * N;
-  const double um = wc.unorm;
-  const double* st = a.stats + (f * a.maxNodes + li) * 3;
-  const double ulo = st[0] / um, uhi = st[1] / um;
-  const int lane = BLOCK ? threadIdx.x : (threadIdx.x & 31);
-  const int step = BLOCK ? blockDim.x : 32;
+// RobustMeanEstimate (noise.hpp:239-270) of one leaf of window w, slice k.
+// The weights of an iteration come from the previous (m, 1/d), so nothing
+// is stored per element; the IQD of r = u - m is (u_hi - m) - (u_lo - m)
+// from the leaf's order statistics.  `val(e)` is the leaf's e-th u value;
+// `lane`/`step`/`sum` describe the cooperating threads (a warp or a CTA).
+template <class V, class R>
+__device__ double robust_mean(V val, int n, double ulo, double uhi, int lane, int step, R sum) {
   double m = 0.0, m0 = 1e12, mprev = 0.0, inv = 0.0;
   for (int it = 0; it < kMaxIter; ++it) {
     double sw = 0.0, swa = 0.0;
     for (int e = lane; e < n; e += step) {
-      const double x = a.src.at(f, q.x + e % N, q.y + e / N) / um;
+      const double x = val(e);
       const double w = it == 0 ? 1.0 : huber((x - mprev) * inv);
       sw += w;
       swa += w * x;
     }
-    if (BLOCK) {
-      sw = block_sum(sw, red);
-      swa = block_sum(swa, red);
-    } else {
-      sw = warp_sum(sw);
-      swa = warp_sum(swa);
-    }
+    sw = sum(sw);
+    swa = sum(swa);
     m = (fabs(sw) < kEps) ? m0 : swa / sw;
     double se = 0.0;
-    for (int e = lane; e < n; e += step)
-      se += fabs(a.src.at(f, q.x + e % N, q.y + e / N) / um - m);
-    se = BLOCK ? block_sum(se, red) : warp_sum(se);
-    const double e_ = se / (double)n;
-    if (fabs(m0 - m) < kTol || e_ < kTol) break;
+    for (int e = lane; e < n; e += step) se += fabs(val(e) - m);
+    se = sum(se);
+    if (fabs(m0 - m) < kTol || se / (double)n < kTol) break;
     m0 = m;
-    const double d = ((uhi - m) - (ulo - m)) + kEps;  // IQD of r = u - m
+    const double d = ((uhi - m) - (ulo - m)) + kEps;
     mprev = m;
     inv = 1.0 / d;
   }
   return m;
 }
 
-__global__ void __launch_bounds__(256) k_leaf_mean_warp(Problem pb, DeviceBuffers d, MeanArgs a) {
-  const int w = blockIdx.z, k = blockIdx.y;
-  const int li = blockIdx.x * 8 + (threadIdx.x >> 5);
+// leaves of side <= 32: one warp each, the leaf's u values (x / umax, as the
+// reference normalises) staged once in shared memory
+__global__ void __launch_bounds__(128) k_leaf_mean_warp(Problem pb, DeviceBuffers d, MeanArgs a) {
+  __shared__ double sbuf[4][1024];
+  const int w = blockIdx.z, k = blockIdx.y, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int li = blockIdx.x * 4 + wib;
   const WinConst& wc = d.wc[w];
   const size_t f = (size_t)(wc.s0 + k);
-  if (li >= a.nleaf[f]) return;
-  if (a.leaf[f * a.maxNodes + li].z > 32) return;  // k_leaf_mean_block
-  const double m = robust_mean<false>(a, wc, k, li, nullptr);
-  if ((threadIdx.x & 31) == 0) a.mean[((size_t)w * a.nwin + k) * a.maxNodes + li] = m;
+  if (li >= a.nleaf[f] || a.dup[f * a.maxNodes + li] >= 0) return;
+  const int4 q = a.leaf[f * a.maxNodes + li];
+  if (q.z > 32) return;  // k_leaf_mean_block
+  const int N = q.z, n = N * N;
+  const double um = wc.unorm;
+  double* buf = sbuf[wib];
+  for (int e = lane; e < n; e += 32) buf[e] = a.src.at(f, q.x + e % N, q.y + e / N) / um;
+  __syncwarp();
+  const double* st = a.stats + (f * a.maxNodes + li) * 3;
+  const double m = robust_mean([&](int e) { return buf[e]; }, n, st[0] / um, st[1] / um, lane,
+                               32, [](double v) { return warp_sum(v); });
+  if (lane == 0) a.mean[((size_t)w * a.nwin + k) * a.maxNodes + li] = m;
 }
 
+// leaves of side > 32: one CTA each
 __global__ void __launch_bounds__(256) k_leaf_mean_block(Problem pb, DeviceBuffers d, MeanArgs a,
                                                          const int* big, const int* nbig) {
   const int w = blockIdx.z, k = blockIdx.y;
@@ -424,12 +455,19 @@ __global__ void __launch_bounds__(256) k_leaf_mean_block(Problem pb, DeviceBuffe
   const size_t f = (size_t)(wc.s0 + k);
   if ((int)blockIdx.x >= nbig[f]) return;
   const int li = big[f * a.maxNodes + blockIdx.x];
+  if (a.dup[f * a.maxNodes + li] >= 0) return;
+  const int4 q = a.leaf[f * a.maxNodes + li];
+  const int N = q.z;
+  const double um = wc.unorm;
   __shared__ double red[32];
-  const double m = robust_mean<true>(a, wc, k, li, red);
+  const double* st = a.stats + (f * a.maxNodes + li) * 3;
+  const double m = robust_mean(
+      [&](int e) { return a.src.at(f, q.x + e % N, q.y + e / N) / um; }, N * N, st[0] / um,
+      st[1] / um, threadIdx.x, blockDim.x, [&](double v) { return block_sum(v, red); });
   if (threadIdx.x == 0) a.mean[((size_t)w * a.nwin + k) * a.maxNodes + li] = m;
 }
 
-// Leaves of side > 32 of each frame (for k_leaf_mean_block).
+// Leaves of side > 32 of each frame (for k_leaf_mean_block / k_leaf_stats_big).
 __global__ void k_big_leaves(const int4* leaf, const int* nleaf, int nimg, int maxNodes, int* big,
                              int* nbig) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -442,22 +480,99 @@ __global__ void k_big_leaves(const int4* leaf, const int* nleaf, int nimg, int m
 
 struct FitArgs {
   const int* nleaf;
+  const int* dup;
   const double* stats;
   const double* mean;
   int maxNodes, nwin, method;
   double* x;        // [W][nwin * maxNodes] leaf means of the window
   double* y;        // leaf variances of the window
+  unsigned long long* key;  // ordered bits of the residuals
   int* hist;        // [W][nwin * maxNodes + 1] mode counts (method 3)
 };
 
-// WLSFit (noise.hpp:302-358) and the method's mu / sigma; the results go to
-// the window constants (caller-side values, then the risk's binding).
-__global__ void __launch_bounds__(1024) k_noise_fit(Problem pb, DeviceBuffers d, FitArgs a) {
-  const int w = blockIdx.x;
+constexpr int kFitCtas = 8;       // CTAs of the cluster that fits one window
+constexpr int kFitThreads = 512;
+constexpr int kDigitBits = 11, kDigits = 1 << kDigitBits;
+
+namespace cg = cooperative_groups;
+
+__device__ double cluster_max(cg::cluster_group& cl, double v, double* red, double* part) {
+  v = block_max(v, red);
+  if (threadIdx.x == 0) *part = v;
+  cl.sync();
+  double t = *cl.map_shared_rank(part, 0);
+  for (int r = 1; r < kFitCtas; ++r) t = fmax(t, *cl.map_shared_rank(part, r));
+  cl.sync();
+  return t;
+}
+
+// Sum over the cluster of one value per CTA thread; every thread of every
+// CTA gets the same total (the CTAs' partials added in rank order).
+__device__ double cluster_sum(cg::cluster_group& cl, double v, double* red, double* part) {
+  v = block_sum(v, red);
+  if (threadIdx.x == 0) *part = v;
+  cl.sync();
+  double t = 0.0;
+  for (int r = 0; r < kFitCtas; ++r) t += *cl.map_shared_rank(part, r);
+  cl.sync();  // the partials may be overwritten afterwards
+  return t;
+}
+
+// k-th smallest (0-based) of the window's N residual keys, 11 bits per pass;
+// each CTA histograms its slice, every CTA adds the cluster's histograms.
+__device__ unsigned long long cluster_select(cg::cluster_group& cl, const unsigned long long* key,
+                                             int lo, int hi, int k, unsigned* hist,
+                                             unsigned* tot) {
+  unsigned long long prefix = 0ull, mask = 0ull;
+  for (int shift = 64 - kDigitBits; shift > -kDigitBits; shift -= kDigitBits) {
+    const int sh = shift < 0 ? 0 : shift;
+    const int bits = shift < 0 ? kDigitBits + shift : kDigitBits;
+    const unsigned dmask = (1u << bits) - 1u;
+    for (int i = threadIdx.x; i < kDigits; i += blockDim.x) hist[i] = 0u;
+    __syncthreads();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const unsigned long long kv = key[i];
+      if ((kv & mask) == prefix) atomicAdd(&hist[(unsigned)(kv >> sh) & dmask], 1u);
+    }
+    cl.sync();
+    for (int i = threadIdx.x; i < kDigits; i += blockDim.x) {
+      unsigned t = 0u;
+      for (int r = 0; r < kFitCtas; ++r) t += cl.map_shared_rank(hist, r)[i];
+      tot[i] = t;
+    }
+    cl.sync();  // every CTA has read every histogram
+    __shared__ int s_dg, s_k;
+    if (threadIdx.x == 0) {
+      int acc = 0, dg = 0;
+      for (; dg < (int)dmask; ++dg) {
+        if (acc + (int)tot[dg] > k) break;
+        acc += (int)tot[dg];
+      }
+      s_dg = dg;
+      s_k = k - acc;
+    }
+    __syncthreads();
+    prefix |= (unsigned long long)s_dg << sh;
+    mask |= (unsigned long long)dmask << sh;
+    k = s_k;
+    __syncthreads();
+  }
+  return prefix;
+}
+
+// WLSFit (noise.hpp:302-358) and the method's mu / sigma for one window, by a
+// cluster of kFitCtas CTAs (distributed shared memory for the reductions);
+// the results go to the window constants (caller-side values, then the
+// risk's binding).
+__global__ void __cluster_dims__(kFitCtas, 1, 1) __launch_bounds__(kFitThreads)
+    k_noise_fit(Problem pb, DeviceBuffers d, FitArgs a) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int w = blockIdx.y;
   WinConst& wc = d.wc[w];
   __shared__ double red[32];
-  __shared__ unsigned hist[256];
-  __shared__ int sh[2];
+  __shared__ double part;
+  __shared__ unsigned hist[kDigits], tot[kDigits];
   __shared__ int base[32];
   const int nwin = a.nwin;
   if (threadIdx.x == 0) {
@@ -470,23 +585,27 @@ __global__ void __launch_bounds__(1024) k_noise_fit(Problem pb, DeviceBuffers d,
   }
   __syncthreads();
   const int N = base[nwin];
+  const int lo = (int)((long long)N * rank / kFitCtas), hi = (int)((long long)N * (rank + 1) / kFitCtas);
   double* X = a.x + (size_t)w * nwin * a.maxNodes;
   double* Y = a.y + (size_t)w * nwin * a.maxNodes;
+  unsigned long long* K = a.key + (size_t)w * nwin * a.maxNodes;
   const double um2 = wc.unorm * wc.unorm;
-  for (int k = 0; k < nwin; ++k) {
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    int k = 0;
+    while (k + 1 < nwin && i >= base[k + 1]) ++k;
     const size_t f = (size_t)(wc.s0 + k);
-    const int nl = a.nleaf[f];
-    for (int li = threadIdx.x; li < nl; li += blockDim.x) {
-      X[base[k] + li] = a.mean[((size_t)w * nwin + k) * a.maxNodes + li];
-      Y[base[k] + li] = a.stats[(f * a.maxNodes + li) * 3 + 2] / um2;
-    }
+    const int li = i - base[k];
+    const int dp = a.dup[f * a.maxNodes + li];
+    const int src = dp >= 0 ? dp : li;
+    X[i] = a.mean[((size_t)w * nwin + k) * a.maxNodes + src];
+    Y[i] = a.stats[(f * a.maxNodes + src) * 3 + 2] / um2;
   }
-  __syncthreads();
+  cl.sync();
   const int mq = ((N + 1) / 2 + 1) / 2;
   double a0 = 1e12, b0 = 1e12, p0 = 0.0, p1 = 0.0, q0 = 0.0, q1 = 0.0, dd = 1.0;
   for (int it = 0; it < kMaxIter; ++it) {
-    double s[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double s[5] = {0, 0, 0, 0, 0};
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const double xi = X[i], yi = Y[i];
       const double wt = it == 0 ? 1.0 : huber((yi - (xi * q0 + q1)) / dd);
       const double w2 = wt * wt;
@@ -496,59 +615,48 @@ __global__ void __launch_bounds__(1024) k_noise_fit(Problem pb, DeviceBuffers d,
       s[3] += w2 * (xi * yi);
       s[4] += w2 * (xi * xi);
     }
-    for (int k = 0; k < 5; ++k) s[k] = block_sum(s[k], red);
+    for (int k = 0; k < 5; ++k) s[k] = cluster_sum(cl, s[k], red, &part);
     p0 = s[0] * s[3] - s[1] * s[2];
     const double aux = s[0] * s[4] - s[1] * s[1];
     p0 = (fabs(aux) < kEps) ? a0 : p0 / aux;
     p1 = s[2] - p0 * s[1];
     p1 = (fabs(aux) < kEps) ? b0 : p1 / s[0];
     double se = 0.0;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) se += fabs(Y[i] - (X[i] * p0 + p1));
-    se = block_sum(se, red) / (double)N;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const double r = Y[i] - (X[i] * p0 + p1);
+      se += fabs(r);
+      K[i] = okey(r);
+    }
+    se = cluster_sum(cl, se, red, &part) / (double)N;  // its syncs also publish K
     if ((fabs(a0 - p0) < kTol && fabs(b0 - p1) < kTol) || se < kTol) break;
     a0 = p0;
     b0 = p1;
-    auto rv = [&](int i) { return Y[i] - (X[i] * p0 + p1); };
-    const double rlo = block_select(rv, N, mq - 1, hist, sh);
-    const double rhi = block_select(rv, N, N - mq - 1, hist, sh);
+    const double rlo = ovalue(cluster_select(cl, K, lo, hi, mq - 1, hist, tot));
+    const double rhi = ovalue(cluster_select(cl, K, lo, hi, N - mq - 1, hist, tot));
     q0 = p0;
     q1 = p1;
     dd = (rhi - rlo) + kEps;
   }
   // mu: smallest leaf mean (method 4) or the mode of the leaf means (3)
   double mn = 1e300, mx = -1e300;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     mn = fmin(mn, X[i]);
     mx = fmax(mx, X[i]);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  }
-  __shared__ double smn[32], smx[32];
-  __shared__ double s_mode;
-  if ((threadIdx.x & 31) == 0) {
-    smn[threadIdx.x >> 5] = mn;
-    smx[threadIdx.x >> 5] = mx;
-  }
-  __syncthreads();
-  mn = smn[0];
-  mx = smx[0];
-  for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
-    mn = fmin(mn, smn[q]);
-    mx = fmax(mx, smx[q]);
-  }
+  mn = -cluster_max(cl, -mn, red, &part);
+  mx = cluster_max(cl, mx, red, &part);
   double mode = 0.0;
   if (a.method == 3) {  // ComputeMode (noise.hpp:272-297) of the leaf means
     int* h = a.hist + (size_t)w * (nwin * a.maxNodes + 1);
     const double dyn = (double)N;
-    for (int i = threadIdx.x; i <= N; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    for (int i = lo + threadIdx.x; i <= (rank + 1 == kFitCtas ? N : hi - 1); i += blockDim.x) h[i] = 0;
+    cl.sync();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const double r = round(X[i] * dyn / mx);
       atomicAdd(&h[(int)fmin(fmax(r, 0.0), dyn)], 1);
     }
-    __syncthreads();
+    cl.sync();
+    __shared__ double s_mode;
     if (threadIdx.x == 0) {  // most frequent rounded value; ties: the smallest
       int best = 0, bc = -1;
       for (int i = 0; i <= N; ++i)
@@ -561,7 +669,7 @@ __global__ void __launch_bounds__(1024) k_noise_fit(Problem pb, DeviceBuffers d,
     __syncthreads();
     mode = s_mode;
   }
-  if (threadIdx.x == 0) {
+  if (rank == 0 && threadIdx.x == 0) {
     const double alpha = pb.alpha_c >= 0 ? pb.alpha_c : p0;
     const double mu = pb.mu_c >= 0 ? pb.mu_c : (a.method == 3 ? mode : mn);
     const double sigma = pb.sigma_c >= 0 ? pb.sigma_c : sqrt(fabs(p1 + p0 * mu));
@@ -599,12 +707,14 @@ cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, in
   if (nsmall > 0)
     k_quad_decide_small<<<dim3((nsmall + 7) / 8, nimg), 256, 0, s>>>(src, nlev, lbig, nf.split);
   k_quad_tree<<<(nimg + 63) / 64, 64, 0, s>>>(nf.split, nimg, S, nlev, nf.maxNodes, nf.nodes,
-                                              nf.isdel, nf.leaf, nf.nleaf, nf.err);
+                                              nf.isdel, nf.leaf, nf.nleaf, nf.dup, nf.first,
+                                              nf.err);
   k_big_leaves<<<(nimg + 63) / 64, 64, 0, s>>>(nf.leaf, nf.nleaf, nimg, nf.maxNodes, nf.big,
                                                nf.nbig);
   k_leaf_stats_small<<<dim3((nf.maxNodes + 3) / 4, nimg), 128, 0, s>>>(src, nf.leaf, nf.nleaf,
-                                                                       nf.maxNodes, nf.stats);
-  k_leaf_stats_big<<<dim3(nf.maxBig, nimg), 256, 0, s>>>(src, nf.leaf, nf.big, nf.nbig,
+                                                                       nf.dup, nf.maxNodes,
+                                                                       nf.stats);
+  k_leaf_stats_big<<<dim3(nf.maxBig, nimg), 256, 0, s>>>(src, nf.leaf, nf.big, nf.nbig, nf.dup,
                                                          nf.maxNodes, nf.stats);
   return cudaGetLastError();
 }
@@ -612,12 +722,13 @@ cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, in
 cudaError_t launch_noise_windows(const Problem& pb, const DeviceBuffers& d, const NoiseFrames& nf,
                                  const NoiseWindows& nw, cudaStream_t s) {
   const Geometry& g = pb.g;
-  MeanArgs ma{FrameSrc{d.xs, d.x64, g.S}, nf.leaf, nf.nleaf, nf.stats, nf.maxNodes, g.nwin,
-              nw.mean};
-  k_leaf_mean_warp<<<dim3((nf.maxNodes + 7) / 8, g.nwin, pb.W), 256, 0, s>>>(pb, d, ma);
+  MeanArgs ma{FrameSrc{d.xs, d.x64, g.S}, nf.leaf, nf.nleaf, nf.dup, nf.stats, nf.maxNodes,
+              g.nwin, nw.mean};
+  k_leaf_mean_warp<<<dim3((nf.maxNodes + 3) / 4, g.nwin, pb.W), 128, 0, s>>>(pb, d, ma);
   k_leaf_mean_block<<<dim3(nf.maxBig, g.nwin, pb.W), 256, 0, s>>>(pb, d, ma, nf.big, nf.nbig);
-  FitArgs fa{nf.nleaf, nf.stats, nw.mean, nf.maxNodes, g.nwin, nw.method, nw.x, nw.y, nw.hist};
-  k_noise_fit<<<pb.W, 1024, 0, s>>>(pb, d, fa);
+  FitArgs fa{nf.nleaf, nf.dup, nf.stats, nw.mean, nf.maxNodes, g.nwin, nw.method, nw.x, nw.y,
+             nw.key, nw.hist};
+  k_noise_fit<<<dim3(kFitCtas, pb.W), kFitThreads, 0, s>>>(pb, d, fa);
   return cudaGetLastError();
 }
 

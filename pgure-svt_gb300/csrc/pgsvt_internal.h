@@ -139,6 +139,7 @@ struct DeviceBuffers {
   const float* zs;         // median-filtered sequence (null: no pre-filter)
   const double* zmax;      // its per-frame maxima
   float* wz;               // [W][nwin][S*S] ARPS input zs / wnorm
+  int int_input;           // every input value an integer <= 2^19 (ARPS integer mode)
   float* u;
   uint32_t* pos;
   const int32_t* plist;    // kept patch -> position index
@@ -187,7 +188,7 @@ struct DeviceBuffers {
 cudaError_t launch_convert(const void* X, int dtype, size_t n, float* xs, double* x64,
                            cudaStream_t s);
 cudaError_t launch_frame_max(const float* xs, const double* x64, int nimg, size_t F,
-                             double* fmax, cudaStream_t s);
+                             double* fmax, cudaStream_t s, int* fint = nullptr);
 cudaError_t launch_median(const float* xs, const double* x64, int nimg, int S, int r, float* zs,
                           cudaStream_t s);
 constexpr int kMaxMedian = 15;     // median pre-filter radius supported
@@ -216,6 +217,8 @@ struct NoiseFrames {
   int* big;         // [nimg][maxNodes] indices of leaves of side > 32
   int* nbig;        // [nimg]
   double* stats;    // [nimg][maxNodes][3] (a_lo, a_hi, var), raw scale
+  int* dup;         // [nimg][maxNodes] earlier leaf with the same block, or -1
+  int* first;       // [nimg][blocks of side >= 8] scratch of the duplicate search
   int* err;         // replay overflow flag
 };
 // ... and per window batch
@@ -224,6 +227,7 @@ struct NoiseWindows {
   double* mean;     // [W][nwin][maxNodes] robust leaf means (normalised)
   double* x;        // [W][nwin * maxNodes] fit inputs
   double* y;
+  unsigned long long* key;  // [W][nwin * maxNodes] ordered residual bits
   int* hist;        // [W][nwin * maxNodes + 1]
 };
 int noise_levels(int S);

@@ -33,35 +33,44 @@ cudaError_t launch_convert(const void* X, int dtype, size_t n, float* xs, double
   return cudaGetLastError();
 }
 
-// Per input frame: maximum (exact) and a flag for negative / non-finite values.
+// Per input frame: maximum (exact), a flag for negative / non-finite values
+// and (fint, optional) whether every value is an integer <= 2^19.
 __global__ void k_frame_max(const float* __restrict__ xs, const double* __restrict__ x64,
-                            size_t F, double* __restrict__ fmx) {
+                            size_t F, double* __restrict__ fmx, int* __restrict__ fint) {
   const int f = blockIdx.x;
   double m = -INFINITY;
-  bool bad = false;
+  bool bad = false, nonint = false;
   for (size_t i = threadIdx.x; i < F; i += blockDim.x) {
     const double v = x64 ? x64[f * F + i] : (double)xs[f * F + i];
     bad |= !(v >= 0.0) || isinf(v);  // NaN, negative or infinite
+    nonint |= !(v <= 524288.0) || v != floor(v);
     m = fmax(m, v);
   }
   __shared__ double sm[32];
-  __shared__ int sbad;
-  if (threadIdx.x == 0) sbad = 0;
+  __shared__ int sbad, snon;
+  if (threadIdx.x == 0) {
+    sbad = 0;
+    snon = 0;
+  }
   __syncthreads();
   if (bad) atomicOr(&sbad, 1);
+  if (nonint) atomicOr(&snon, 1);
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
     m = (threadIdx.x < blockDim.x / 32) ? sm[threadIdx.x] : -INFINITY;
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0) fmx[f] = sbad ? -1.0 : m;  // -1 marks an invalid frame
+    if (threadIdx.x == 0) {
+      fmx[f] = sbad ? -1.0 : m;  // -1 marks an invalid frame
+      if (fint) fint[f] = snon ? 0 : 1;
+    }
   }
 }
 
 cudaError_t launch_frame_max(const float* xs, const double* x64, int nimg, size_t F,
-                             double* fmax, cudaStream_t s) {
-  k_frame_max<<<nimg, 512, 0, s>>>(xs, x64, F, fmax);
+                             double* fmax, cudaStream_t s, int* fint) {
+  k_frame_max<<<nimg, 512, 0, s>>>(xs, x64, F, fmax, fint);
   return cudaGetLastError();
 }
 

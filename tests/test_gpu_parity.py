@@ -259,3 +259,17 @@ def test_denoise_with_median_prefilter_matches_oracle(capi, oracle, g):
     # and the filter changed the trajectories
     Y1, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.1, n_jobs=4)
     assert np.abs(Y1 - Y0).max() > 1e-3 * np.abs(Y0).max()
+
+
+def test_integer_input_arps_ties_match_oracle(capi, oracle, pkg):
+    # integer-valued input: ARPS compares exact integer sums of squared
+    # differences and settles equal sums as the reference's FP64 costs do;
+    # coarse quantisation makes flat regions, hence many exact ties
+    clean = pkg.synth.blobs(40, 18, 10, seed=3) / 25.0
+    X = np.asfortranarray(np.round(clean).astype(np.uint16))
+    p = capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1)
+    Y, _, st = capi.denoise(X, p)
+    Y0, _, _ = oracle.denoise(X.astype(np.float64), median_size=-1, optimize_pgure=0,
+                              lambda_=0.1, n_jobs=4)
+    print("FP64 tie decisions:", st.arps_exact_steps)
+    assert np.abs(Y - Y0).max() < 2e-5 * np.abs(Y0).max()
