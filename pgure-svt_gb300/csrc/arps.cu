@@ -25,6 +25,8 @@ struct ArpsCtx {
   const float* xa2;
   const double* xa1d; // input frames when the input is f64
   const double* xa2d;
+  const double* pa1;  // FP64 normalised slices when precomputed (median
+  const double* pa2;  // pre-filter: ties are frequent), else null
   double umax;
   int S;
   int mw;
@@ -120,8 +122,9 @@ __device__ double cost64(const ArpsCtx& c, int i, int j, int y, int x) {
 #pragma unroll
   for (int e = 0; e < BS * BS; ++e) {
     const int r = e % BS, cc = e / BS;
-    const double a = __ddiv_rn(src64(c, c.xa1, c.xa1d, (i + r) + (size_t)(j + cc) * c.S), c.umax);
-    const double b = __ddiv_rn(src64(c, c.xa2, c.xa2d, (y + r) + (size_t)(x + cc) * c.S), c.umax);
+    const size_t ka = (i + r) + (size_t)(j + cc) * c.S, kb = (y + r) + (size_t)(x + cc) * c.S;
+    const double a = c.pa1 ? c.pa1[ka] : __ddiv_rn(src64(c, c.xa1, c.xa1d, ka), c.umax);
+    const double b = c.pa2 ? c.pa2[kb] : __ddiv_rn(src64(c, c.xa2, c.xa2d, kb), c.umax);
     const double d = __dsub_rn(a, b);
     const double sq = __dmul_rn(d, d);
     if (e & 1) v2 = __dadd_rn(v2, sq);
@@ -334,6 +337,8 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
     c.xa2 = xw + (size_t)(wc.s0 + a2) * F;
     c.xa1d = xd ? xd + (size_t)(wc.s0 + a1) * F : nullptr;
     c.xa2d = xd ? xd + (size_t)(wc.s0 + a2) * F : nullptr;
+    c.pa1 = d.w64 ? d.w64 + ((size_t)w * g.nwin + a1) * F : nullptr;
+    c.pa2 = d.w64 ? d.w64 + ((size_t)w * g.nwin + a2) * F : nullptr;
     int oy, ox;
     arps_pair<BS>(c, it, my, mx, oy, ox, d.counters);
     d.pos[((size_t)w * g.nwin + a2) * g.P + it] = (uint32_t)oy | ((uint32_t)ox << 16);

@@ -367,7 +367,7 @@ size_t window_bytes(const Problem& pb) {
   const size_t C = g.cube(), NP = g.NP, NC = g.NC;
   size_t b = 0;
   b += C * 4;                       // u
-  b += C * 4;                       // wz (median pre-filter; counted always)
+  b += C * 12;                      // wz, w64 (median pre-filter; counted always)
   b += (size_t)g.nwin * g.P * 4;    // pos
   b += C * 4;                       // cnt
   b += C * 4 * 3;                   // fields
@@ -635,7 +635,10 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.zs = zs;
     d.zmax = zmx;
     d.int_input = int_input;
-    if (zs) d.wz = mem.arr<float>((size_t)W * C);
+    if (zs) {
+      d.wz = mem.arr<float>((size_t)W * C);
+      d.w64 = mem.arr<double>((size_t)W * C);
+    }
     d.plist = plist;
     d.counters = counters;
     d.Y = Y_dev;

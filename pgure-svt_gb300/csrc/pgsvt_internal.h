@@ -139,6 +139,7 @@ struct DeviceBuffers {
   const float* zs;         // median-filtered sequence (null: no pre-filter)
   const double* zmax;      // its per-frame maxima
   float* wz;               // [W][nwin][S*S] ARPS input zs / wnorm
+  double* w64;             // [W][nwin][S*S] the same in FP64 (the reference's values)
   int int_input;           // every input value an integer <= 2^19 (ARPS integer mode)
   float* u;
   uint32_t* pos;

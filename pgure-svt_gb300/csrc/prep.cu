@@ -202,10 +202,13 @@ __global__ void k_window_norm(Problem pb, DeviceBuffers d) {
   }
   if (d.zs) {  // ARPS input from the median-filtered sequence
     float* wz = d.wz + (size_t)w * C;
+    double* w64 = d.w64 + (size_t)w * C;
     const float wn = (float)c.wnorm;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < C;
-         i += (size_t)gridDim.x * blockDim.x)
+         i += (size_t)gridDim.x * blockDim.x) {
       wz[i] = __fdiv_rn(d.zs[base + i], wn);
+      w64[i] = (double)d.zs[base + i] / c.wnorm;  // pguresvt.hpp:117-120
+    }
   }
 }
 
