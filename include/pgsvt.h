@@ -324,6 +324,15 @@ int pgsvt_risk_window(const double* u, uint32_t nrows, uint32_t nwin,
 int pgsvt_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nrows, uint32_t ncols,
                         uint32_t nframes, uint32_t r);
 
+/* Hot-pixel filter of the command-line tool (HotPixelFilter,
+ * hotpixel.hpp:19-64, applied by PGURE-SVT.cpp:170-176 when `hot_pixel` is
+ * set), in place on `nframes` uint16 frames (host, nrows x ncols x nframes,
+ * column-major): per frame, pixels farther than threshold x MAD (median
+ * absolute deviation / 0.6745) from the median are replaced by the mean of
+ * the middle two of their 8 neighbours, or by the median at the frame edge. */
+int pgsvt_hot_pixel_filter(uint16_t* frames, uint32_t nrows, uint32_t ncols, uint32_t nframes,
+                           double threshold);
+
 /* Singular values of one window without any device allocation.
  *
  * This entry point has no counterpart in the reference.  It serves callers

@@ -98,6 +98,7 @@ def lib():
             ctypes.c_void_p]
         L.orc_noise_estimate.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 4 + [
             P(ctypes.c_double)] * 3
+        L.orc_hot_pixel.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [ctypes.c_double]
         L.orc_median_filter.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3
         L.orc_denoise.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [
             P(OrcParams), ctypes.c_void_p, ctypes.c_void_p, P(OrcReport)]
@@ -211,6 +212,16 @@ def noise_estimate(u, method=4, alpha=-1.0, mu=-1.0, sigma=-1.0):
     _check(lib().orc_noise_estimate(_ptr(u), u.shape[0], u.shape[1], u.shape[2], method,
                                     ctypes.byref(a), ctypes.byref(m), ctypes.byref(s)))
     return a.value, m.value, s.value
+
+
+def hot_pixel_filter(frames, threshold):
+    """HotPixelFilter on uint16 frames (rows, cols[, frames]); returns a copy."""
+    a = np.array(frames, dtype=np.uint16, order="F", copy=True)
+    shp = a.shape
+    if a.ndim == 2:
+        a = a.reshape(shp[0], shp[1], 1, order="F")
+    _check(lib().orc_hot_pixel(_ptr(a), a.shape[0], a.shape[1], a.shape[2], float(threshold)))
+    return a.reshape(shp, order="F")
 
 
 def median_filter(frame, r):

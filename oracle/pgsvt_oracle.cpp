@@ -867,6 +867,55 @@ int orc_noise_estimate(const double* u, uint32_t nrows, uint32_t ncols, uint32_t
   });
 }
 
+// HotPixelFilter (hotpixel.hpp:19-64) on uint16 frames, in place, with the
+// element-type semantics of Armadillo 9.880.1 (not in the reference tree):
+// medians of uint16 data are uint16 (even count: lo + (hi - lo)/2 in integer
+// arithmetic); `slice - median` and `... > threshold * mad` convert the double
+// operand to uint16 and compute in uint16 (differences wrap modulo 65536).
+int orc_hot_pixel(uint16_t* seq, uint32_t nr, uint32_t nc, uint32_t nimg, double thr) {
+  return guarded([&] {
+    auto med16 = [](std::vector<uint16_t> v) -> uint16_t {
+      const size_t n = v.size(), h = n / 2;
+      std::nth_element(v.begin(), v.begin() + h, v.end());
+      if (n % 2) return v[h];
+      const uint16_t lo = *std::max_element(v.begin(), v.begin() + h);
+      return (uint16_t)(lo + (uint16_t)((v[h] - lo) / 2));
+    };
+    auto med_of_cols = [&](const uint16_t* a, uint16_t sub) {
+      std::vector<uint16_t> cm(nc), col(nr);
+      for (uint32_t c = 0; c < nc; ++c) {
+        for (uint32_t r = 0; r < nr; ++r) col[r] = (uint16_t)(a[r + (size_t)c * nr] - sub);
+        cm[c] = med16(col);
+      }
+      return med16(cm);
+    };
+    for (uint32_t f = 0; f < nimg; ++f) {
+      uint16_t* a = seq + (size_t)f * nr * nc;
+      const double median = (double)med_of_cols(a, 0);
+      const uint16_t mu16 = (uint16_t)median;
+      const double mad = (double)med_of_cols(a, mu16) * (1.0 / 0.6745);
+      const double t = thr * mad;
+      const uint16_t tu = !(t > 0.0) ? 0 : (t >= 65535.0 ? 65535 : (uint16_t)t);
+      std::vector<size_t> out;
+      for (size_t i = 0; i < (size_t)nr * nc; ++i)
+        if ((uint16_t)(a[i] - mu16) > tu) out.push_back(i);
+      for (size_t i : out) {
+        const uint32_t r = (uint32_t)(i % nr), c = (uint32_t)(i / nr);
+        if (r > 0 && r < nr - 1 && c > 0 && c < nc - 1) {
+          double w[8] = {(double)a[(r - 1) + (size_t)(c - 1) * nr], (double)a[(r - 1) + (size_t)c * nr],
+                         (double)a[(r - 1) + (size_t)(c + 1) * nr], (double)a[r + (size_t)(c - 1) * nr],
+                         (double)a[r + (size_t)(c + 1) * nr], (double)a[(r + 1) + (size_t)(c - 1) * nr],
+                         (double)a[(r + 1) + (size_t)c * nr], (double)a[(r + 1) + (size_t)(c + 1) * nr]};
+          std::sort(w, w + 8);
+          a[i] = (uint16_t)(0.5 * (w[3] + w[4]));
+        } else {
+          a[i] = (uint16_t)median;
+        }
+      }
+    }
+  });
+}
+
 int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,
                       uint32_t r) {
   return guarded([&] { median_frame(src, dst, (int)nx, (int)ny, (int)r); });

@@ -86,6 +86,10 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs,
 int orc_noise_estimate(const double* u, uint32_t nrows, uint32_t ncols, uint32_t nslices,
                        uint32_t method, double* alpha, double* mu, double* sigma);
 
+/* Hot-pixel filter (hotpixel.hpp:19-64), in place on uint16 frames. */
+int orc_hot_pixel(uint16_t* seq, uint32_t nrows, uint32_t ncols, uint32_t nframes,
+                  double threshold);
+
 /* Median of the (2r+1)^2 window with clamped coordinates (the reference's
  * ConstantTimeMedianFilter, medfilter.hpp:478-541); nx is the fast axis. */
 int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t ny,

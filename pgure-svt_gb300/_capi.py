@@ -28,7 +28,7 @@ COMPAT_ALL = 0x7
 EXPORTS = ("pgsvt_default_params", "pgsvt_denoise", "pgsvt_denoise_device",
            "pgsvt_denoise_ex", "pgsvt_denoise_device_ex", "pgsvt_lambda_predict",
            "pgsvt_lambda_grad", "pgsvt_lambda_train", "pgsvt_denoise_batch",
-           "pgsvt_median_filter",
+           "pgsvt_median_filter", "pgsvt_hot_pixel_filter",
            "pgsvt_arps_window", "pgsvt_svd_window", "pgsvt_reconstruct_window",
            "pgsvt_risk_window", "pgsvt_svd_window_noalloc", "pgsvt_last_error",
            "pgsvt_version")
@@ -132,6 +132,7 @@ def load(path=LIB_PATH):
     L.pgsvt_lambda_predict.argtypes = [vp, vp, u32, vp]
     L.pgsvt_denoise_batch.argtypes = [vp, u32, u32, P(Status)]
     L.pgsvt_median_filter.argtypes = [vp, vp, u32, u32, u32, u32]
+    L.pgsvt_hot_pixel_filter.argtypes = [vp, u32, u32, u32, dbl]
     L.pgsvt_lambda_grad.argtypes = [vp, vp, vp, u32, vp, P(dbl)]
     L.pgsvt_lambda_train.argtypes = [vp, vp, vp, u32, P(TrainParams), vp, P(Status)]
     L.pgsvt_arps_window.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, i32, u32, vp, vp]
@@ -256,6 +257,17 @@ def median_filter(frames, r):
     out = np.zeros_like(a, order="F")
     _check(load().pgsvt_median_filter(_ptr(a), _ptr(out), a.shape[0], a.shape[1], a.shape[2], r))
     return out.reshape(shp, order="F")
+
+
+def hot_pixel_filter(frames, threshold):
+    """pgsvt_hot_pixel_filter on uint16 frames (rows, cols[, frames]); returns a copy."""
+    a = np.array(frames, dtype=np.uint16, order="F", copy=True)
+    shp = a.shape
+    if a.ndim == 2:
+        a = a.reshape(shp[0], shp[1], 1, order="F")
+    _check(load().pgsvt_hot_pixel_filter(_ptr(a), a.shape[0], a.shape[1], a.shape[2],
+                                         float(threshold)))
+    return a.reshape(shp, order="F")
 
 
 def _f32(a, shape=None):

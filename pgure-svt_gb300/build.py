@@ -2,7 +2,8 @@
 
 Every translation unit under csrc/ is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked into
-``pgure-svt_gb300/libpgsvt.so`` next to this file.  nvcc cross-compiles without
+``pgure-svt_gb300/libpgsvt.so`` next to this file; the command-line tool
+``cli/pgsvt_cli.cpp`` (host C++ on the C ABI) becomes ``pgure-svt_gb300/pgsvt_cli``.  nvcc cross-compiles without
 a GPU, so the same recipe runs on a build host and on the GPU machine.
 """
 import concurrent.futures
@@ -17,8 +18,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpgsvt.so")
 SOURCES = ["prep.cu", "arps.cu", "svd.cu", "svd_i0.cu", "svd_i1.cu", "svd_i2.cu", "svd_i3.cu",
            "svd_i4.cu", "svd_i5.cu", "svd_i6.cu", "svd_i7.cu", "svd_s0.cu", "svd_s1.cu",
-           "svd_s2.cu", "svd_s3.cu", "eval.cu", "lambda.cu", "noise.cu", "capi.cu",
-           "noalloc.cu"]
+           "svd_s2.cu", "svd_s3.cu", "eval.cu", "lambda.cu", "noise.cu", "hotpixel.cu",
+           "capi.cu", "noalloc.cu"]
+CLI_SRC = os.path.join(HERE, "cli", "pgsvt_cli.cpp")
+CLI = os.path.join(HERE, "pgsvt_cli")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -74,6 +77,12 @@ def build(force=False, verbose=False, ptxas_verbose=False):
         tmp = LIB + ".tmp%d" % os.getpid()
         run([nvcc()] + ARCH + ["-shared", "-cudart=static", "-o", tmp] + objs)
         os.replace(tmp, LIB)
+    # the command-line tool: host C++ on the C ABI, next to the library
+    if force or _stale(CLI, [CLI_SRC, LIB, os.path.join(ROOT, "include", "pgsvt.h")]):
+        tmp = CLI + ".tmp%d" % os.getpid()
+        run(["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), CLI_SRC,
+             "-L", HERE, "-lpgsvt", "-Wl,-rpath,$ORIGIN", "-o", tmp])
+        os.replace(tmp, CLI)
     return LIB
 
 

@@ -1357,6 +1357,31 @@ int pgsvt_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nrows, uint
   });
 }
 
+int pgsvt_hot_pixel_filter(uint16_t* frames, uint32_t nrows, uint32_t ncols, uint32_t nframes,
+                           double threshold) {
+  return guarded(nullptr, [&](Stats& stats) {
+    if (!frames) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
+    if (!(threshold >= 0.0)) throw Fail(PGSVT_ERR_INVALID_ARG, "threshold must be >= 0");
+    if (nrows == 0 || ncols == 0 || nframes == 0) return;
+    need_device();
+    const size_t F = (size_t)nrows * ncols, n = F * nframes;
+    DevMem mem;
+    cudaStream_t s;
+    PGSVT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    uint16_t* seq = mem.arr<uint16_t>(n);
+    uint16_t* colmed = mem.arr<uint16_t>((size_t)ncols * nframes);
+    uint32_t* med = mem.arr<uint32_t>(nframes);
+    uint32_t* madm = mem.arr<uint32_t>(nframes);
+    uint8_t* flag = mem.arr<uint8_t>(n);
+    PGSVT_CK(cudaMemcpyAsync(seq, frames, n * 2, cudaMemcpyHostToDevice, s));
+    check_launch(launch_hot_pixel(seq, (int)nrows, (int)ncols, (int)nframes, threshold, colmed,
+                                  med, madm, flag, s), stats, 6);
+    PGSVT_CK(cudaMemcpyAsync(frames, seq, n * 2, cudaMemcpyDeviceToHost, s));
+    PGSVT_CK(cudaStreamSynchronize(s));
+  });
+}
+
 int pgsvt_arps_window(const double* w, uint32_t nrows, uint32_t nwin, uint32_t block_size,
                       uint32_t motion_window, uint32_t time_iter, uint32_t frame_window,
                       uint32_t nimages, int32_t motion_estimation, uint32_t compat_flags,

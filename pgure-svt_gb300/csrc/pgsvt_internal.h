@@ -238,6 +238,10 @@ cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, in
 cudaError_t launch_noise_windows(const Problem& pb, const DeviceBuffers& d, const NoiseFrames& nf,
                                  const NoiseWindows& nw, cudaStream_t s);
 
+// hot-pixel filter (hotpixel.cu)
+cudaError_t launch_hot_pixel(uint16_t* seq, int nr, int nc, int nimg, double thr, uint16_t* colmed,
+                             uint32_t* med, uint32_t* madm, uint8_t* flag, cudaStream_t s);
+
 // learned lambda proposal (lambda.cu)
 struct LambdaTrain {
   float* m;            // FP32 model (PGSVT_LAMBDA_MODEL_FLOATS)
