@@ -530,6 +530,72 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   if (fb == 0 && fe == 0) fe = nimg;
   if (fb < 0 || fe > nimg || fb >= fe) throw Fail(PGSVT_ERR_INVALID_ARG, "bad frame range");
   const int nwinds = fe - fb;
+  // noise estimates of every window before the batches (noise.cu): leaf
+  // means once per (frame, window maximum) pair, then one fit per window
+  double* est_win = nullptr;
+  if (estimate) {
+    std::vector<int> win_s0(nwinds), win_pair((size_t)nwinds * g.nwin), pair_frame;
+    std::vector<double> win_norm(nwinds), pair_norm;
+    std::map<std::pair<int, double>, int> pid;
+    for (int k = 0; k < nwinds; ++k) {
+      const int t = fb + k;
+      const int s0 = t < g.fw ? 0 : (t >= nimg - g.fw ? nimg - 2 * g.fw - 1 : t - g.fw);
+      double um = hmax[s0];
+      for (int q = 1; q < g.nwin; ++q) um = std::max(um, hmax[s0 + q]);
+      um = um > 0.0 ? um : 1.0;  // the window's normalisation (WinConst::unorm)
+      win_s0[k] = s0;
+      win_norm[k] = um;
+      for (int q = 0; q < g.nwin; ++q) {
+        const auto key = std::make_pair(s0 + q, um);
+        auto it = pid.find(key);
+        if (it == pid.end()) {
+          it = pid.emplace(key, (int)pair_frame.size()).first;
+          pair_frame.push_back(s0 + q);
+          pair_norm.push_back(um);
+        }
+        win_pair[(size_t)k * g.nwin + q] = it->second;
+      }
+    }
+    NoisePass np{};
+    np.method = (int)p.noise_method;
+    np.npairs = (int)pair_frame.size();
+    np.nwin = g.nwin;
+    np.alpha_c = p.alpha;
+    np.mu_c = p.mu;
+    np.sigma_c = p.sigma;
+    auto up = [&](const auto& v) {
+      using T = typename std::decay_t<decltype(v)>::value_type;
+      T* dptr = mem.arr<T>(v.size());
+      PGSVT_CK(cudaMemcpyAsync(dptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+      stats.h2d += sizeof(T) * v.size();
+      return dptr;
+    };
+    np.pair_frame = up(pair_frame);
+    np.pair_norm = up(pair_norm);
+    np.mean = mem.arr<double>((size_t)np.npairs * nf.maxNodes);
+    int* d_win_pair = up(win_pair);
+    int* d_win_s0 = up(win_s0);
+    double* d_win_norm = up(win_norm);
+    est_win = mem.arr<double>((size_t)nwinds * 3);
+    // windows in chunks, the fit scratch reused
+    const int chunk = std::min(nwinds, 64);
+    const size_t per_w = (size_t)g.nwin * nf.maxNodes;
+    np.x = mem.arr<double>(chunk * per_w);
+    np.y = mem.arr<double>(chunk * per_w);
+    np.key = mem.arr<unsigned long long>(chunk * per_w);
+    np.hist = mem.arr<int>(chunk * (per_w + 1));
+    for (int k0 = 0; k0 < nwinds; k0 += chunk) {
+      NoisePass npc = np;
+      npc.nwindows = std::min(chunk, nwinds - k0);
+      npc.win_pair = d_win_pair + (size_t)k0 * g.nwin;
+      npc.win_s0 = d_win_s0 + k0;
+      npc.win_norm = d_win_norm + k0;
+      npc.est = est_win + (size_t)k0 * 3;
+      if (k0 > 0) npc.npairs = 0;  // the leaf means are computed once
+      check_launch(launch_noise_pass(nf, npc, xs, x64, S, s), stats, k0 > 0 ? 1 : 3);
+    }
+    PGSVT_CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  }
   // batch size: about half a million kept patches per batch
   int W = p.window_batch ? (int)p.window_batch
                          : (int)std::max<int64_t>(1, (500000 + g.NP - 1) / (int64_t)g.NP);
@@ -607,7 +673,6 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } evg{ready};
   PGSVT_CK(cudaEventRecord(ready, s));
 
-  std::vector<NoiseWindows> nws(NS);
   std::vector<Lane> lanes(NS);
   struct LaneGuard {
     std::vector<Lane>& l;
@@ -670,16 +735,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.part_mse = mem.arr<double>(std::max<size_t>((size_t)W * pb.K * d.nblk_mse, (size_t)W * 256));
     d.wc = mem.arr<WinConst>(W);
     d.st = mem.arr<SearchState>(W);
-    if (estimate) {
-      NoiseWindows& nw = nws[li];
-      nw.method = (int)p.noise_method;
-      const size_t per = (size_t)g.nwin * nf.maxNodes;
-      nw.mean = mem.arr<double>((size_t)W * per);
-      nw.x = mem.arr<double>((size_t)W * per);
-      nw.y = mem.arr<double>((size_t)W * per);
-      nw.key = mem.arr<unsigned long long>((size_t)W * per);
-      nw.hist = mem.arr<int>((size_t)W * (per + 1));
-    }
+
     d.model = dmodel;
     d.model_bf16 = dmodel_bf;
     d.feat_slots = fslots;
@@ -730,7 +786,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     }
     clk.mark(7);  // probe uploads and other gaps
     check_launch(launch_window_setup(pbb, d, L.s), stats, 2);
-    if (estimate) check_launch(launch_noise_windows(pbb, d, nf, nws[bi % NS], L.s), stats, 3);
+    if (estimate) check_launch(launch_noise_apply(pbb, d, est_win, fb, L.s), stats);
     clk.mark(1);
     check_launch(launch_arps(pbb, d, L.s), stats, pbb.motion ? 2 : 1);
     clk.mark(2);

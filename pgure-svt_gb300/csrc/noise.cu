@@ -14,22 +14,28 @@
 // GB300 mapping.  The split decisions and the leaf variances are
 // scale-equivariant, so they are computed once per input frame on the raw
 // values and rescaled per window (var_u = var_x / umax^2); the robust means
-// (whose stopping tolerance is absolute) and the fit run per window:
+// depend on the window only through its maximum (their stopping tolerance is
+// absolute), so they run once per (frame, distinct window maximum) pair, and
+// every window then fits its own line:
 //   k_quad_decide   one CTA per (frame, block of side > 8): the F statistic
 //   k_quad_tree     one thread per frame: replays the reference's recursion
 //                   over the decision table, including its quirks (the
 //                   node that was last before a split is re-visited, the
 //                   fourth child is not; the smallest split index, the root,
 //                   stays a leaf), and lists the leaves in its order
-//   k_leaf_stats    one CTA per (frame, leaf): order statistics by 8-bit
-//                   radix selection (IQD bounds, Laplacian median and MAD)
-//   k_leaf_mean     one warp per (window, slice, leaf of side <= 32, values
-//                   staged in shared memory), one CTA per larger leaf: the
-//                   IRLS robust mean; the recursion lists most blocks twice,
-//                   and every repeated block reuses the first one's results
-//   k_noise_fit     one cluster of 8 CTAs per window (distributed shared
-//                   memory for the sums and the radix selections): the IRLS
-//                   fit, mu, sigma
+//   k_leaf_stats    per (frame, unique leaf): order statistics (IQD bounds,
+//                   Laplacian median and MAD) by warp bitonic sorts in shared
+//                   memory (sides <= 32) or by a cluster of 8 CTAs with
+//                   11-bit radix selection over distributed shared memory
+//   k_leaf_mean     per (frame, window maximum) pair: one warp per leaf of
+//                   side <= 32, one cluster of 8 CTAs per larger leaf: the
+//                   IRLS robust mean, on the raw values with the absolute
+//                   tolerances scaled by the window maximum; the recursion
+//                   lists most blocks twice, and every repeated block reuses
+//                   the first one's results
+//   k_noise_fit     one cluster of 8 CTAs per window, all windows in one
+//                   launch (distributed shared memory for the sums and the
+//                   radix selections): the IRLS fit, mu, sigma
 // All arithmetic is FP64.
 #include <cooperative_groups.h>
 
@@ -347,127 +353,281 @@ __global__ void __launch_bounds__(128) k_leaf_stats_small(FrameSrc src, const in
   }
 }
 
-// The same for leaves of side > 32: one CTA per leaf, radix selection.
-__global__ void __launch_bounds__(256) k_leaf_stats_big(FrameSrc src, const int4* leaf,
-                                                        const int* big, const int* nbig,
-                                                        const int* dup, int maxNodes,
-                                                        double* stats) {
-  const int f = blockIdx.y;
-  if ((int)blockIdx.x >= nbig[f]) return;
-  const int li = big[(size_t)f * maxNodes + blockIdx.x];
+// ---- cluster helpers (distributed shared memory across kCl CTAs)
+
+constexpr int kCl = 8;            // CTAs per cluster
+constexpr int kClThreads = 512;
+constexpr int kDigitBits = 11, kDigits = 1 << kDigitBits;
+
+namespace cg = cooperative_groups;
+
+struct ClusterSmem {
+  double red[32];
+  double part[8];
+  unsigned h[2][kDigits];   // this CTA's histograms
+  unsigned t[2][kDigits];   // the cluster's
+  int dg[2], kk[2];
+  int scan[kClThreads / 32 + 1];
+};
+
+// Sums over the cluster of up to 8 values per thread; every thread of every
+// CTA gets the same totals (the CTAs' partials added in rank order).
+template <int NV>
+__device__ void cluster_sums(cg::cluster_group& cl, double (&v)[NV], ClusterSmem& sm) {
+  for (int k = 0; k < NV; ++k) {
+    const double b = block_sum(v[k], sm.red);
+    if (threadIdx.x == 0) sm.part[k] = b;
+  }
+  cl.sync();
+  for (int k = 0; k < NV; ++k) {
+    double t = 0.0;
+    for (int r = 0; r < kCl; ++r) t += cl.map_shared_rank(sm.part, r)[k];
+    v[k] = t;
+  }
+  cl.sync();  // the partials may be overwritten afterwards
+}
+
+__device__ double cluster_max(cg::cluster_group& cl, double v, ClusterSmem& sm) {
+  const double b = block_max(v, sm.red);
+  if (threadIdx.x == 0) sm.part[0] = b;
+  cl.sync();
+  double t = *cl.map_shared_rank(sm.part, 0);
+  for (int r = 1; r < kCl; ++r) t = fmax(t, cl.map_shared_rank(sm.part, r)[0]);
+  cl.sync();
+  return t;
+}
+
+// The digit of the k-th smallest key among the counts t[0..nb): a block-wide
+// prefix scan (each thread owns nb / blockDim consecutive bins).
+__device__ void find_digit(const unsigned* t, int nb, int k, int* out_dg, int* out_k, int* scan) {
+  const int per = (nb + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  int loc = 0;
+  for (int b = b0; b < b0 + per && b < nb; ++b) loc += (int)t[b];
+  // exclusive scan of loc over the block
+  int inc = loc;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) scan[wid] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      const int v = scan[q];
+      scan[q] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  int before = scan[wid] + inc - loc;
+  if (before <= k && k < before + loc) {
+    for (int b = b0; b < b0 + per && b < nb; ++b) {
+      if (before + (int)t[b] > k) {
+        *out_dg = b;
+        *out_k = k - before;
+        break;
+      }
+      before += (int)t[b];
+    }
+  }
+  __syncthreads();
+}
+
+// The k0-th and k1-th smallest of the n keys key(i) spread over the cluster
+// (this CTA holds the indices [lo, hi)), 11 bits per pass.
+template <class K>
+__device__ void cluster_select2(cg::cluster_group& cl, K key, int lo, int hi, int k0, int k1,
+                                ClusterSmem& sm, unsigned long long& v0, unsigned long long& v1) {
+  unsigned long long pre[2] = {0ull, 0ull}, mask = 0ull;
+  int k[2] = {k0, k1};
+  for (int shift = 64 - kDigitBits; shift > -kDigitBits; shift -= kDigitBits) {
+    const int sh = shift < 0 ? 0 : shift;
+    const int bits = shift < 0 ? kDigitBits + shift : kDigitBits;
+    const unsigned dm = (1u << bits) - 1u;
+    for (int b = threadIdx.x; b < kDigits; b += blockDim.x) sm.h[0][b] = sm.h[1][b] = 0u;
+    __syncthreads();
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const unsigned long long kv = key(i);
+      const unsigned dgt = (unsigned)(kv >> sh) & dm;
+      if ((kv & mask) == pre[0]) atomicAdd(&sm.h[0][dgt], 1u);
+      if ((kv & mask) == pre[1]) atomicAdd(&sm.h[1][dgt], 1u);
+    }
+    cl.sync();
+    for (int b = threadIdx.x; b <= (int)dm; b += blockDim.x) {
+      unsigned t0 = 0u, t1 = 0u;
+      for (int r = 0; r < kCl; ++r) {
+        const ClusterSmem* rs = cl.map_shared_rank(&sm, r);
+        t0 += rs->h[0][b];
+        t1 += rs->h[1][b];
+      }
+      sm.t[0][b] = t0;
+      sm.t[1][b] = t1;
+    }
+    cl.sync();  // every CTA has read every histogram
+    for (int q = 0; q < 2; ++q) find_digit(sm.t[q], (int)dm + 1, k[q], &sm.dg[q], &sm.kk[q], sm.scan);
+    for (int q = 0; q < 2; ++q) {
+      pre[q] |= (unsigned long long)sm.dg[q] << sh;
+      k[q] = sm.kk[q];
+    }
+    mask |= (unsigned long long)dm << sh;
+    __syncthreads();
+  }
+  v0 = pre[0];
+  v1 = pre[1];
+}
+
+// Armadillo median() from the two middle keys of an even count
+__device__ __forceinline__ double median_from(unsigned long long lo, unsigned long long hi, int n) {
+  if (n % 2) return ovalue(hi);
+  const double a = ovalue(lo), b = ovalue(hi);
+  return a + (b - a) / 2.0;
+}
+
+// Per (frame, unique leaf of side > 32): the leaf statistics of
+// k_leaf_stats_small by one cluster per leaf.
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads)
+    k_leaf_stats_big(FrameSrc src, const int4* leaf, const int* big, const int* nbig,
+                     const int* dup, int maxNodes, double* stats) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), bi = blockIdx.x / kCl, f = blockIdx.y;
+  __shared__ ClusterSmem sm;
+  const bool valid = bi < nbig[f];  // uniform over the cluster
+  if (!valid) return;
+  const int li = big[(size_t)f * maxNodes + bi];
   if (dup[(size_t)f * maxNodes + li] >= 0) return;
   const int4 q = leaf[(size_t)f * maxNodes + li];
   const int N = q.z, n = N * N;
-  __shared__ unsigned hist[256];
-  __shared__ int sh[2];
+  const int lo = (int)((long long)n * rank / kCl), hi = (int)((long long)n * (rank + 1) / kCl);
   auto A = [&](int r, int c) { return src.at(f, q.x + r, q.y + c); };
-  auto aval = [&](int e) { return A(e % N, e / N); };
   const int m = iqd_m(n);
-  const double alo = block_select(aval, n, m - 1, hist, sh);
-  const double ahi = block_select(aval, n, n - m - 1, hist, sh);
-  auto lap = [&](int e) { return lap_at(A, e, N); };
-  auto median_of = [&](auto fv) {
-    if (n % 2) return block_select(fv, n, n / 2, hist, sh);
-    const double lo = block_select(fv, n, n / 2 - 1, hist, sh);
-    const double hi = block_select(fv, n, n / 2, hist, sh);
-    return lo + (hi - lo) / 2.0;
-  };
-  const double med = median_of(lap);
-  auto dev = [&](int e) { return fabs(lap(e) - med); };
-  const double mad = median_of(dev);
-  if (threadIdx.x == 0) {
+  unsigned long long a0, a1, l0, l1, d0, d1;
+  cluster_select2(cl, [&](int e) { return okey(A(e % N, e / N)); }, lo, hi, m - 1, n - m - 1, sm,
+                  a0, a1);
+  const int mlo = n % 2 ? n / 2 : n / 2 - 1;
+  cluster_select2(cl, [&](int e) { return okey(lap_at(A, e, N)); }, lo, hi, mlo, n / 2, sm, l0, l1);
+  const double med = median_from(l0, l1, n);
+  cluster_select2(cl, [&](int e) { return okey(fabs(lap_at(A, e, N) - med)); }, lo, hi, mlo,
+                  n / 2, sm, d0, d1);
+  const double mad = median_from(d0, d1, n);
+  if (rank == 0 && threadIdx.x == 0) {
     const double sig = 1.4826 * mad;
     double* o = stats + ((size_t)f * maxNodes + li) * 3;
-    o[0] = alo;
-    o[1] = ahi;
+    o[0] = ovalue(a0);
+    o[1] = ovalue(a1);
     o[2] = sig * sig;
   }
 }
 
-struct MeanArgs {
-  FrameSrc src;
-  const int4* leaf;
-  const int* nleaf;
-  const int* dup;
-  const double* stats;
-  int maxNodes, nwin;
-  double* mean;  // [W][nwin][maxNodes]
-};
-
-// RobustMeanEstimate (noise.hpp:239-270) of one leaf of window w, slice k.
-// The weights of an iteration come from the previous (m, 1/d), so nothing
-// is stored per element; the IQD of r = u - m is (u_hi - m) - (u_lo - m)
-// from the leaf's order statistics.  `val(e)` is the leaf's e-th u value;
-// `lane`/`step`/`sum` describe the cooperating threads (a warp or a CTA).
+// RobustMeanEstimate (noise.hpp:239-270) of one leaf, run on the raw values
+// x = u * um: with u = x / um every step is the same up to rounding when the
+// absolute constants scale with um (tol, eps; the weights are scale-free),
+// so m_u = m_x / um without dividing every element.  The weights of an
+// iteration come from the previous (m, 1/d), so nothing is stored per
+// element; the IQD of r = x - m is (x_hi - m) - (x_lo - m) from the leaf's
+// order statistics.  `sum(a, b, c)` reduces three values over the
+// cooperating threads (a warp, or a cluster).
 template <class V, class R>
-__device__ double robust_mean(V val, int n, double ulo, double uhi, int lane, int step, R sum) {
-  double m = 0.0, m0 = 1e12, mprev = 0.0, inv = 0.0;
+__device__ double robust_mean(V val, int lo, int hi, int n, double xlo, double xhi, double um,
+                              int lane, int step, R sum) {
+  const double tol = kTol * um, eps = kEps * um;
+  double m = 0.0, m0 = 1e12 * um, mprev = 0.0, inv = 0.0;
   for (int it = 0; it < kMaxIter; ++it) {
     double sw = 0.0, swa = 0.0;
-    for (int e = lane; e < n; e += step) {
+    for (int e = lo + lane; e < hi; e += step) {
       const double x = val(e);
       const double w = it == 0 ? 1.0 : huber((x - mprev) * inv);
       sw += w;
       swa += w * x;
     }
-    sw = sum(sw);
-    swa = sum(swa);
-    m = (fabs(sw) < kEps) ? m0 : swa / sw;
     double se = 0.0;
-    for (int e = lane; e < n; e += step) se += fabs(val(e) - m);
-    se = sum(se);
-    if (fabs(m0 - m) < kTol || se / (double)n < kTol) break;
+    // e = mean |x - m| needs m first: a second pass after the reduction
+    sum(sw, swa, se, false);
+    m = (fabs(sw) < kEps) ? m0 : swa / sw;
+    for (int e = lo + lane; e < hi; e += step) se += fabs(val(e) - m);
+    sum(sw, swa, se, true);
+    if (fabs(m0 - m) < tol || se / (double)n < tol) break;
     m0 = m;
-    const double d = ((uhi - m) - (ulo - m)) + kEps;
+    const double d = ((xhi - m) - (xlo - m)) + eps;
     mprev = m;
     inv = 1.0 / d;
   }
-  return m;
+  return m / um;
 }
 
-// leaves of side <= 32: one warp each, the leaf's u values (x / umax, as the
-// reference normalises) staged once in shared memory
-__global__ void __launch_bounds__(128) k_leaf_mean_warp(Problem pb, DeviceBuffers d, MeanArgs a) {
-  __shared__ double sbuf[4][1024];
-  const int w = blockIdx.z, k = blockIdx.y, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int li = blockIdx.x * 4 + wib;
-  const WinConst& wc = d.wc[w];
-  const size_t f = (size_t)(wc.s0 + k);
+struct PairArgs {
+  FrameSrc src;
+  const int4* leaf;
+  const int* nleaf;
+  const int* dup;
+  const int* big;
+  const int* nbig;
+  const double* stats;
+  int maxNodes;
+  const int* pair_frame;     // [npairs]
+  const double* pair_norm;   // [npairs] normalisation of the pair (window maximum)
+  double* mean;              // [npairs][maxNodes]
+};
+
+// robust means of the leaves of side <= 32 of every (frame, normalisation)
+// pair: one warp per leaf
+__global__ void __launch_bounds__(128) k_leaf_mean_warp(PairArgs a) {
+  const int pr = blockIdx.y, lane = threadIdx.x & 31;
+  const int li = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const size_t f = (size_t)a.pair_frame[pr];
   if (li >= a.nleaf[f] || a.dup[f * a.maxNodes + li] >= 0) return;
   const int4 q = a.leaf[f * a.maxNodes + li];
-  if (q.z > 32) return;  // k_leaf_mean_block
-  const int N = q.z, n = N * N;
-  const double um = wc.unorm;
-  double* buf = sbuf[wib];
-  for (int e = lane; e < n; e += 32) buf[e] = a.src.at(f, q.x + e % N, q.y + e / N) / um;
-  __syncwarp();
-  const double* st = a.stats + (f * a.maxNodes + li) * 3;
-  const double m = robust_mean([&](int e) { return buf[e]; }, n, st[0] / um, st[1] / um, lane,
-                               32, [](double v) { return warp_sum(v); });
-  if (lane == 0) a.mean[((size_t)w * a.nwin + k) * a.maxNodes + li] = m;
-}
-
-// leaves of side > 32: one CTA each
-__global__ void __launch_bounds__(256) k_leaf_mean_block(Problem pb, DeviceBuffers d, MeanArgs a,
-                                                         const int* big, const int* nbig) {
-  const int w = blockIdx.z, k = blockIdx.y;
-  const WinConst& wc = d.wc[w];
-  const size_t f = (size_t)(wc.s0 + k);
-  if ((int)blockIdx.x >= nbig[f]) return;
-  const int li = big[f * a.maxNodes + blockIdx.x];
-  if (a.dup[f * a.maxNodes + li] >= 0) return;
-  const int4 q = a.leaf[f * a.maxNodes + li];
+  if (q.z > 32) return;  // k_leaf_mean_big
   const int N = q.z;
-  const double um = wc.unorm;
-  __shared__ double red[32];
+  const double um = a.pair_norm[pr];
   const double* st = a.stats + (f * a.maxNodes + li) * 3;
   const double m = robust_mean(
-      [&](int e) { return a.src.at(f, q.x + e % N, q.y + e / N) / um; }, N * N, st[0] / um,
-      st[1] / um, threadIdx.x, blockDim.x, [&](double v) { return block_sum(v, red); });
-  if (threadIdx.x == 0) a.mean[((size_t)w * a.nwin + k) * a.maxNodes + li] = m;
+      [&](int e) { return a.src.at(f, q.x + e % N, q.y + e / N); }, 0, N * N, N * N, st[0], st[1],
+      um, lane, 32, [](double& x, double& y, double& z, bool zonly) {
+        if (zonly) {
+          z = warp_sum(z);
+        } else {
+          x = warp_sum(x);
+          y = warp_sum(y);
+        }
+      });
+  if (lane == 0) a.mean[(size_t)pr * a.maxNodes + li] = m;
 }
 
-// Leaves of side > 32 of each frame (for k_leaf_mean_block / k_leaf_stats_big).
+// ... and of the leaves of side > 32: one cluster per leaf
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads)
+    k_leaf_mean_big(PairArgs a) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), bi = blockIdx.x / kCl, pr = blockIdx.y;
+  const size_t f = (size_t)a.pair_frame[pr];
+  if (bi >= a.nbig[f]) return;  // uniform over the cluster
+  const int li = a.big[f * a.maxNodes + bi];
+  if (a.dup[f * a.maxNodes + li] >= 0) return;
+  __shared__ ClusterSmem sm;
+  const int4 q = a.leaf[f * a.maxNodes + li];
+  const int N = q.z, n = N * N;
+  const int lo = (int)((long long)n * rank / kCl), hi = (int)((long long)n * (rank + 1) / kCl);
+  const double* st = a.stats + (f * a.maxNodes + li) * 3;
+  const double m = robust_mean(
+      [&](int e) { return a.src.at(f, q.x + e % N, q.y + e / N); }, lo, hi, n, st[0], st[1],
+      a.pair_norm[pr], threadIdx.x, blockDim.x, [&](double& x, double& y, double& z, bool zonly) {
+        if (zonly) {
+          double v[1] = {z};
+          cluster_sums(cl, v, sm);
+          z = v[0];
+        } else {
+          double v[2] = {x, y};
+          cluster_sums(cl, v, sm);
+          x = v[0];
+          y = v[1];
+        }
+      });
+  if (rank == 0 && threadIdx.x == 0) a.mean[(size_t)pr * a.maxNodes + li] = m;
+}
+
+// Leaves of side > 32 of each frame.
 __global__ void k_big_leaves(const int4* leaf, const int* nleaf, int nimg, int maxNodes, int* big,
                              int* nbig) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -482,122 +642,51 @@ struct FitArgs {
   const int* nleaf;
   const int* dup;
   const double* stats;
-  const double* mean;
+  const double* mean;        // [npairs][maxNodes]
+  const int* win_pair;       // [nwindows][nwin] pair of (window, slice)
+  const int* win_s0;         // [nwindows] first frame of the window
+  const double* win_norm;    // [nwindows] window normalisation
   int maxNodes, nwin, method;
-  double* x;        // [W][nwin * maxNodes] leaf means of the window
-  double* y;        // leaf variances of the window
-  unsigned long long* key;  // ordered bits of the residuals
-  int* hist;        // [W][nwin * maxNodes + 1] mode counts (method 3)
+  double alpha_c, mu_c, sigma_c;  // caller values (< 0: estimate)
+  double* x;                 // [nwindows][nwin * maxNodes] scratch
+  double* y;
+  unsigned long long* key;
+  int* hist;                 // [nwindows][nwin * maxNodes + 1]
+  double* est;               // [nwindows][3] caller-side (alpha, mu, sigma)
 };
 
-constexpr int kFitCtas = 8;       // CTAs of the cluster that fits one window
-constexpr int kFitThreads = 512;
-constexpr int kDigitBits = 11, kDigits = 1 << kDigitBits;
-
-namespace cg = cooperative_groups;
-
-__device__ double cluster_max(cg::cluster_group& cl, double v, double* red, double* part) {
-  v = block_max(v, red);
-  if (threadIdx.x == 0) *part = v;
-  cl.sync();
-  double t = *cl.map_shared_rank(part, 0);
-  for (int r = 1; r < kFitCtas; ++r) t = fmax(t, *cl.map_shared_rank(part, r));
-  cl.sync();
-  return t;
-}
-
-// Sum over the cluster of one value per CTA thread; every thread of every
-// CTA gets the same total (the CTAs' partials added in rank order).
-__device__ double cluster_sum(cg::cluster_group& cl, double v, double* red, double* part) {
-  v = block_sum(v, red);
-  if (threadIdx.x == 0) *part = v;
-  cl.sync();
-  double t = 0.0;
-  for (int r = 0; r < kFitCtas; ++r) t += *cl.map_shared_rank(part, r);
-  cl.sync();  // the partials may be overwritten afterwards
-  return t;
-}
-
-// k-th smallest (0-based) of the window's N residual keys, 11 bits per pass;
-// each CTA histograms its slice, every CTA adds the cluster's histograms.
-__device__ unsigned long long cluster_select(cg::cluster_group& cl, const unsigned long long* key,
-                                             int lo, int hi, int k, unsigned* hist,
-                                             unsigned* tot) {
-  unsigned long long prefix = 0ull, mask = 0ull;
-  for (int shift = 64 - kDigitBits; shift > -kDigitBits; shift -= kDigitBits) {
-    const int sh = shift < 0 ? 0 : shift;
-    const int bits = shift < 0 ? kDigitBits + shift : kDigitBits;
-    const unsigned dmask = (1u << bits) - 1u;
-    for (int i = threadIdx.x; i < kDigits; i += blockDim.x) hist[i] = 0u;
-    __syncthreads();
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      const unsigned long long kv = key[i];
-      if ((kv & mask) == prefix) atomicAdd(&hist[(unsigned)(kv >> sh) & dmask], 1u);
-    }
-    cl.sync();
-    for (int i = threadIdx.x; i < kDigits; i += blockDim.x) {
-      unsigned t = 0u;
-      for (int r = 0; r < kFitCtas; ++r) t += cl.map_shared_rank(hist, r)[i];
-      tot[i] = t;
-    }
-    cl.sync();  // every CTA has read every histogram
-    __shared__ int s_dg, s_k;
-    if (threadIdx.x == 0) {
-      int acc = 0, dg = 0;
-      for (; dg < (int)dmask; ++dg) {
-        if (acc + (int)tot[dg] > k) break;
-        acc += (int)tot[dg];
-      }
-      s_dg = dg;
-      s_k = k - acc;
-    }
-    __syncthreads();
-    prefix |= (unsigned long long)s_dg << sh;
-    mask |= (unsigned long long)dmask << sh;
-    k = s_k;
-    __syncthreads();
-  }
-  return prefix;
-}
-
-// WLSFit (noise.hpp:302-358) and the method's mu / sigma for one window, by a
-// cluster of kFitCtas CTAs (distributed shared memory for the reductions);
-// the results go to the window constants (caller-side values, then the
-// risk's binding).
-__global__ void __cluster_dims__(kFitCtas, 1, 1) __launch_bounds__(kFitThreads)
-    k_noise_fit(Problem pb, DeviceBuffers d, FitArgs a) {
+// WLSFit (noise.hpp:302-358) and the method's mu / sigma for every window:
+// one cluster per window.
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_noise_fit(FitArgs a) {
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank();
-  const int w = blockIdx.y;
-  WinConst& wc = d.wc[w];
-  __shared__ double red[32];
-  __shared__ double part;
-  __shared__ unsigned hist[kDigits], tot[kDigits];
+  const int rank = (int)cl.block_rank(), w = blockIdx.y;
+  __shared__ ClusterSmem sm;
   __shared__ int base[32];
-  const int nwin = a.nwin;
+  const int nwin = a.nwin, s0 = a.win_s0[w];
   if (threadIdx.x == 0) {
     int t = 0;
     for (int k = 0; k < nwin; ++k) {
       base[k] = t;
-      t += a.nleaf[wc.s0 + k];
+      t += a.nleaf[s0 + k];
     }
     base[nwin] = t;
   }
   __syncthreads();
   const int N = base[nwin];
-  const int lo = (int)((long long)N * rank / kFitCtas), hi = (int)((long long)N * (rank + 1) / kFitCtas);
-  double* X = a.x + (size_t)w * nwin * a.maxNodes;
-  double* Y = a.y + (size_t)w * nwin * a.maxNodes;
-  unsigned long long* K = a.key + (size_t)w * nwin * a.maxNodes;
-  const double um2 = wc.unorm * wc.unorm;
+  const int lo = (int)((long long)N * rank / kCl), hi = (int)((long long)N * (rank + 1) / kCl);
+  const size_t per = (size_t)nwin * a.maxNodes;
+  double* X = a.x + (size_t)w * per;
+  double* Y = a.y + (size_t)w * per;
+  unsigned long long* K = a.key + (size_t)w * per;
+  const double um = a.win_norm[w], um2 = um * um;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     int k = 0;
     while (k + 1 < nwin && i >= base[k + 1]) ++k;
-    const size_t f = (size_t)(wc.s0 + k);
+    const size_t f = (size_t)(s0 + k);
     const int li = i - base[k];
     const int dp = a.dup[f * a.maxNodes + li];
     const int src = dp >= 0 ? dp : li;
-    X[i] = a.mean[((size_t)w * nwin + k) * a.maxNodes + src];
+    X[i] = a.mean[(size_t)a.win_pair[(size_t)w * nwin + k] * a.maxNodes + src];
     Y[i] = a.stats[(f * a.maxNodes + src) * 3 + 2] / um2;
   }
   cl.sync();
@@ -615,27 +704,27 @@ __global__ void __cluster_dims__(kFitCtas, 1, 1) __launch_bounds__(kFitThreads)
       s[3] += w2 * (xi * yi);
       s[4] += w2 * (xi * xi);
     }
-    for (int k = 0; k < 5; ++k) s[k] = cluster_sum(cl, s[k], red, &part);
+    cluster_sums(cl, s, sm);
     p0 = s[0] * s[3] - s[1] * s[2];
     const double aux = s[0] * s[4] - s[1] * s[1];
     p0 = (fabs(aux) < kEps) ? a0 : p0 / aux;
     p1 = s[2] - p0 * s[1];
     p1 = (fabs(aux) < kEps) ? b0 : p1 / s[0];
-    double se = 0.0;
+    double se[1] = {0.0};
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const double r = Y[i] - (X[i] * p0 + p1);
-      se += fabs(r);
+      se[0] += fabs(r);
       K[i] = okey(r);
     }
-    se = cluster_sum(cl, se, red, &part) / (double)N;  // its syncs also publish K
-    if ((fabs(a0 - p0) < kTol && fabs(b0 - p1) < kTol) || se < kTol) break;
+    cluster_sums(cl, se, sm);  // its syncs also publish K
+    if ((fabs(a0 - p0) < kTol && fabs(b0 - p1) < kTol) || se[0] / (double)N < kTol) break;
     a0 = p0;
     b0 = p1;
-    const double rlo = ovalue(cluster_select(cl, K, lo, hi, mq - 1, hist, tot));
-    const double rhi = ovalue(cluster_select(cl, K, lo, hi, N - mq - 1, hist, tot));
+    unsigned long long r0, r1;
+    cluster_select2(cl, [&](int i) { return K[i]; }, lo, hi, mq - 1, N - mq - 1, sm, r0, r1);
     q0 = p0;
     q1 = p1;
-    dd = (rhi - rlo) + kEps;
+    dd = (ovalue(r1) - ovalue(r0)) + kEps;
   }
   // mu: smallest leaf mean (method 4) or the mode of the leaf means (3)
   double mn = 1e300, mx = -1e300;
@@ -643,18 +732,20 @@ __global__ void __cluster_dims__(kFitCtas, 1, 1) __launch_bounds__(kFitThreads)
     mn = fmin(mn, X[i]);
     mx = fmax(mx, X[i]);
   }
-  mn = -cluster_max(cl, -mn, red, &part);
-  mx = cluster_max(cl, mx, red, &part);
+  mn = -cluster_max(cl, -mn, sm);
+  mx = cluster_max(cl, mx, sm);
   double mode = 0.0;
   if (a.method == 3) {  // ComputeMode (noise.hpp:272-297) of the leaf means
-    int* h = a.hist + (size_t)w * (nwin * a.maxNodes + 1);
+    int* h = a.hist + (size_t)w * (per + 1);
     const double dyn = (double)N;
-    for (int i = lo + threadIdx.x; i <= (rank + 1 == kFitCtas ? N : hi - 1); i += blockDim.x) h[i] = 0;
+    for (int i = lo + threadIdx.x; i < (rank + 1 == kCl ? N + 1 : hi); i += blockDim.x) h[i] = 0;
+    __threadfence();
     cl.sync();
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const double r = round(X[i] * dyn / mx);
       atomicAdd(&h[(int)fmin(fmax(r, 0.0), dyn)], 1);
     }
+    __threadfence();
     cl.sync();
     __shared__ double s_mode;
     if (threadIdx.x == 0) {  // most frequent rounded value; ties: the smallest
@@ -670,20 +761,33 @@ __global__ void __cluster_dims__(kFitCtas, 1, 1) __launch_bounds__(kFitThreads)
     mode = s_mode;
   }
   if (rank == 0 && threadIdx.x == 0) {
-    const double alpha = pb.alpha_c >= 0 ? pb.alpha_c : p0;
-    const double mu = pb.mu_c >= 0 ? pb.mu_c : (a.method == 3 ? mode : mn);
-    const double sigma = pb.sigma_c >= 0 ? pb.sigma_c : sqrt(fabs(p1 + p0 * mu));
-    wc.est_alpha = alpha;
-    wc.est_mu = mu;
-    wc.est_sigma = sigma;
-    wc.alpha = alpha;  // PGURE(u, p, alpha, sigma, mu, ...) binding (pgure.hpp:26-30)
-    if (pb.compat & PGSVT_COMPAT_SWAP_MU_SIGMA) {
-      wc.mu = sigma;
-      wc.sigma = mu;
-    } else {
-      wc.mu = mu;
-      wc.sigma = sigma;
-    }
+    const double alpha = a.alpha_c >= 0 ? a.alpha_c : p0;
+    const double mu = a.mu_c >= 0 ? a.mu_c : (a.method == 3 ? mode : mn);
+    const double sigma = a.sigma_c >= 0 ? a.sigma_c : sqrt(fabs(p1 + p0 * mu));
+    a.est[(size_t)w * 3] = alpha;
+    a.est[(size_t)w * 3 + 1] = mu;
+    a.est[(size_t)w * 3 + 2] = sigma;
+  }
+}
+
+// The estimates of a window batch into its window constants: caller-side
+// values, then the risk's binding PGURE(u, p, alpha, sigma, mu, ...)
+// (pgure.hpp:26-30).
+__global__ void k_noise_apply(Problem pb, DeviceBuffers d, const double* est, int win0) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= pb.W) return;
+  WinConst& wc = d.wc[w];
+  const double* e = est + (size_t)(wc.t - win0) * 3;
+  wc.est_alpha = e[0];
+  wc.est_mu = e[1];
+  wc.est_sigma = e[2];
+  wc.alpha = e[0];
+  if (pb.compat & PGSVT_COMPAT_SWAP_MU_SIGMA) {
+    wc.mu = e[2];
+    wc.sigma = e[1];
+  } else {
+    wc.mu = e[1];
+    wc.sigma = e[2];
   }
 }
 
@@ -714,21 +818,29 @@ cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, in
   k_leaf_stats_small<<<dim3((nf.maxNodes + 3) / 4, nimg), 128, 0, s>>>(src, nf.leaf, nf.nleaf,
                                                                        nf.dup, nf.maxNodes,
                                                                        nf.stats);
-  k_leaf_stats_big<<<dim3(nf.maxBig, nimg), 256, 0, s>>>(src, nf.leaf, nf.big, nf.nbig, nf.dup,
-                                                         nf.maxNodes, nf.stats);
+  k_leaf_stats_big<<<dim3(kCl * nf.maxBig, nimg), kClThreads, 0, s>>>(
+      src, nf.leaf, nf.big, nf.nbig, nf.dup, nf.maxNodes, nf.stats);
   return cudaGetLastError();
 }
 
-cudaError_t launch_noise_windows(const Problem& pb, const DeviceBuffers& d, const NoiseFrames& nf,
-                                 const NoiseWindows& nw, cudaStream_t s) {
-  const Geometry& g = pb.g;
-  MeanArgs ma{FrameSrc{d.xs, d.x64, g.S}, nf.leaf, nf.nleaf, nf.dup, nf.stats, nf.maxNodes,
-              g.nwin, nw.mean};
-  k_leaf_mean_warp<<<dim3((nf.maxNodes + 3) / 4, g.nwin, pb.W), 128, 0, s>>>(pb, d, ma);
-  k_leaf_mean_block<<<dim3(nf.maxBig, g.nwin, pb.W), 256, 0, s>>>(pb, d, ma, nf.big, nf.nbig);
-  FitArgs fa{nf.nleaf, nf.dup, nf.stats, nw.mean, nf.maxNodes, g.nwin, nw.method, nw.x, nw.y,
-             nw.key, nw.hist};
-  k_noise_fit<<<dim3(kFitCtas, pb.W), kFitThreads, 0, s>>>(pb, d, fa);
+cudaError_t launch_noise_pass(const NoiseFrames& nf, const NoisePass& np, const float* xs,
+                              const double* x64, int S, cudaStream_t s) {
+  PairArgs pa{FrameSrc{xs, x64, S}, nf.leaf, nf.nleaf, nf.dup, nf.big, nf.nbig, nf.stats,
+              nf.maxNodes, np.pair_frame, np.pair_norm, np.mean};
+  if (np.npairs > 0) {
+    k_leaf_mean_warp<<<dim3((nf.maxNodes + 3) / 4, np.npairs), 128, 0, s>>>(pa);
+    k_leaf_mean_big<<<dim3(kCl * nf.maxBig, np.npairs), kClThreads, 0, s>>>(pa);
+  }
+  FitArgs fa{nf.nleaf, nf.dup, nf.stats, np.mean, np.win_pair, np.win_s0, np.win_norm,
+             nf.maxNodes, np.nwin, np.method, np.alpha_c, np.mu_c, np.sigma_c, np.x, np.y,
+             np.key, np.hist, np.est};
+  k_noise_fit<<<dim3(kCl, np.nwindows), kClThreads, 0, s>>>(fa);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_noise_apply(const Problem& pb, const DeviceBuffers& d, const double* est,
+                               int win0, cudaStream_t s) {
+  k_noise_apply<<<(pb.W + 63) / 64, 64, 0, s>>>(pb, d, est, win0);
   return cudaGetLastError();
 }
 

@@ -222,21 +222,30 @@ struct NoiseFrames {
   int* first;       // [nimg][blocks of side >= 8] scratch of the duplicate search
   int* err;         // replay overflow flag
 };
-// ... and per window batch
-struct NoiseWindows {
-  int method;
-  double* mean;     // [W][nwin][maxNodes] robust leaf means (normalised)
-  double* x;        // [W][nwin * maxNodes] fit inputs
+// ... and the windows' estimates, before the denoising batches
+struct NoisePass {
+  int method, npairs, nwindows, nwin;
+  double alpha_c, mu_c, sigma_c;  // caller values (< 0: estimate)
+  const int* pair_frame;     // [npairs] frame of each (frame, window maximum) pair
+  const double* pair_norm;   // [npairs] its window maximum
+  double* mean;              // [npairs][maxNodes] robust leaf means (normalised)
+  const int* win_pair;       // [nwindows][nwin] pair of each (window, slice)
+  const int* win_s0;         // [nwindows] first frame
+  const double* win_norm;    // [nwindows] window maximum
+  double* x;                 // [nwindows][nwin * maxNodes] fit scratch
   double* y;
-  unsigned long long* key;  // [W][nwin * maxNodes] ordered residual bits
-  int* hist;        // [W][nwin * maxNodes + 1]
+  unsigned long long* key;
+  int* hist;                 // [nwindows][nwin * maxNodes + 1]
+  double* est;               // [nwindows][3] (alpha, mu, sigma), caller-side
 };
 int noise_levels(int S);
 int noise_blocks(int nlev);
 cudaError_t launch_noise_frames(const float* xs, const double* x64, int nimg, int S,
                                 const NoiseFrames& nf, cudaStream_t s);
-cudaError_t launch_noise_windows(const Problem& pb, const DeviceBuffers& d, const NoiseFrames& nf,
-                                 const NoiseWindows& nw, cudaStream_t s);
+cudaError_t launch_noise_pass(const NoiseFrames& nf, const NoisePass& np, const float* xs,
+                              const double* x64, int S, cudaStream_t s);
+cudaError_t launch_noise_apply(const Problem& pb, const DeviceBuffers& d, const double* est,
+                               int win0, cudaStream_t s);
 
 // hot-pixel filter (hotpixel.cu)
 cudaError_t launch_hot_pixel(uint16_t* seq, int nr, int nc, int nimg, double thr, uint16_t* colmed,
