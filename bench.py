@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--hint", type=float, default=-1.0, help="fixed lambda proposal")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-lambda arm")
+    ap.add_argument("--no-default-path", action="store_true",
+                    help="skip timing the reference's default path (median 5 + noise estimation)")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time pgsvt_denoise_batch on this many uneven sequences")
     ap.add_argument("--autotune", type=int, default=1,
@@ -411,6 +413,27 @@ def main():
             "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8),
             "svd_variant": {0: "registers", 1: "more lanes per patch",
                             2: "shared memory"}.get(int(st.svd_variant), "?")}
+    if not args.no_default_path:
+        # the reference's default configuration (SVT() / PGURE-SVT defaults):
+        # median pre-filter 5, noise parameters estimated per window, PGURE on
+        pd = capi.default_params(traj_length=15, block_size=args.patch, motion_window=7,
+                                 median_size=5, random_seed=7, autotune=args.autotune)
+        step(pd)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        std_ = step(pd)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        dms = g0.elapsed_time(g1)
+        line["default_path"] = {"value": nimg / (dms / 1e3), "unit": "frames/s",
+                                "ms_per_step": dms, "steps": 1,
+                                "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F")),
+                                "noise_estimates_frame0": [float(v) for v in
+                                                           est.cpu().numpy().reshape(4, nimg)[1:, 0]],
+                                "config": "median filter 5, alpha/mu/sigma estimated "
+                                          "(noise method 4), PGURE on, same sequence"}
     if args.batch:
         line["batch"] = run_batch(capi, args.batch, args.seed)
     if not args.no_cpu_baseline:
