@@ -35,6 +35,8 @@ def nvcc():
 def _flags(ptxas_verbose=False):
     f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                 "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    # developer knob for kernel experiments, e.g. PGSVT_NVCC_FLAGS="-DPGSVT_SVD_PRED"
+    f += os.environ.get("PGSVT_NVCC_FLAGS", "").split()
     if ptxas_verbose:
         f += ["-Xptxas", "-v"]
     return f
