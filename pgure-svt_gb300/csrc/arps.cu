@@ -30,33 +30,50 @@ struct ArpsCtx {
   double umax;
   int S;
   int mw;
+  int bs;             // patch side (used when the kernel is not specialised)
 };
 
+// The reference block of one position.  BS > 0: its values in registers;
+// BS == 0 (patch sides above 8): read from the frame where needed.
 template <int BS>
 struct Block {
-  float ref[BS * BS];  // normalised values, or the raw integers in integer mode
+  float ref[BS > 0 ? BS * BS : 1];  // normalised values, or the raw integers in integer mode
+  const float* src = nullptr;       // BS == 0: the block's first element
+  int S = 0;
+
+  __device__ __forceinline__ float at(int e, int nb) const {
+    if constexpr (BS > 0) return ref[e];
+    else return __ldg(src + (e % nb) + (size_t)(e / nb) * S);
+  }
 
   __device__ void load(const ArpsCtx& c, int i, int j) {
-    const float* src = c.integer ? c.xa1 : c.fa1;
+    const float* sp = c.integer ? c.xa1 : c.fa1;
+    if constexpr (BS > 0) {
 #pragma unroll
-    for (int cc = 0; cc < BS; ++cc)
+      for (int cc = 0; cc < BS; ++cc)
 #pragma unroll
-      for (int r = 0; r < BS; ++r) ref[r + cc * BS] = __ldg(src + (i + r) + (size_t)(j + cc) * c.S);
+        for (int r = 0; r < BS; ++r) ref[r + cc * BS] = __ldg(sp + (i + r) + (size_t)(j + cc) * c.S);
+    } else {
+      src = sp + i + (size_t)j * c.S;
+      S = c.S;
+    }
   }
 
   // Integer mode: the exact sum of squared differences D.  The reference's
   // FP64 cost is D / (umax^2 m) up to an absolute error below
   // (m + 7) 2^-53 (values <= 1 after normalisation), while two different D
   // differ by at least 1 / (umax^2 m) > 2 (m + 7) 2^-53 for umax <= 2^19 and
-  // m <= 64: comparing D decides exactly as the reference does, except for
+  // m <= 64, or umax <= 2^17 and m <= 256 (the host enables the mode only
+  // then): comparing D decides exactly as the reference does, except for
   // equal D.
   __device__ double ssd(const ArpsCtx& c, int y, int x) const {
+    const int nb = BS > 0 ? BS : c.bs;
     unsigned long long acc = 0ull;
 #pragma unroll
-    for (int cc = 0; cc < BS; ++cc)
+    for (int cc = 0; cc < nb; ++cc)
 #pragma unroll
-      for (int r = 0; r < BS; ++r) {
-        const int a = (int)ref[r + cc * BS];
+      for (int r = 0; r < nb; ++r) {
+        const int a = (int)at(r + cc * nb, nb);
         const int b = (int)__ldg(c.xa2 + (y + r) + (size_t)(x + cc) * c.S);
         const long long d = a - b;
         acc += (unsigned long long)(d * d);
@@ -66,11 +83,12 @@ struct Block {
 
   // the candidate block at (y, x) equals the one at (y2, x2), element by element
   __device__ bool same(const ArpsCtx& c, int y, int x, int y2, int x2) const {
+    const int nb = BS > 0 ? BS : c.bs;
     bool eq = true;
 #pragma unroll
-    for (int cc = 0; cc < BS; ++cc)
+    for (int cc = 0; cc < nb; ++cc)
 #pragma unroll
-      for (int r = 0; r < BS; ++r)
+      for (int r = 0; r < nb; ++r)
         eq &= __ldg(c.xa2 + (y + r) + (size_t)(x + cc) * c.S) ==
               __ldg(c.xa2 + (y2 + r) + (size_t)(x2 + cc) * c.S);
     return eq;
@@ -88,24 +106,30 @@ struct Block {
     }
   }
 
-  // FP32 cost and a bound on |cost32 - cost64|:
-  //   2^-24 * (24 * sum_e (|a_e|+|b_e|)^2 / m + 2 * cost)
+  // FP32 cost and a bound on |cost32 - cost64| (u = 2^-24, m = bs^2): the
+  // FP32 operands differ from the reference's FP64 ones by <= 2u|a| (the
+  // normalisation divides by the FP32-rounded maximum), so every difference
+  // by <= 3u(|a|+|b|) and every square by <= 6u(|a|+|b|)^2; the m-term FMA
+  // sum adds <= m u sum d^2 = m^2 u cost.  With margin:
+  //   err = u * (8 * sum_e (|a_e|+|b_e|)^2 / m + (m + 4) * cost)
   __device__ void cost32(const ArpsCtx& c, int y, int x, float& cost, float& err) const {
+    const int nb = BS > 0 ? BS : c.bs;
     float acc = 0.f, sb = 0.f;
 #pragma unroll
-    for (int cc = 0; cc < BS; ++cc)
+    for (int cc = 0; cc < nb; ++cc)
 #pragma unroll
-      for (int r = 0; r < BS; ++r) {
-        const float a = ref[r + cc * BS];
+      for (int r = 0; r < nb; ++r) {
+        const float a = at(r + cc * nb, nb);
         const float b = __ldg(c.fa2 + (y + r) + (size_t)(x + cc) * c.S);
         const float d = a - b;
         acc = fmaf(d, d, acc);
         const float s = fabsf(a) + fabsf(b);
         sb = fmaf(s, s, sb);
       }
-    const float oo = 1.0f / (float)(BS * BS);
+    const float m = (float)(nb * nb);
+    const float oo = 1.0f / m;
     cost = acc * oo;
-    err = 5.9604645e-8f * (24.f * sb * oo + 2.f * cost);
+    err = 5.9604645e-8f * (8.f * sb * oo + (m + 4.f) * cost);
   }
 };
 
@@ -117,11 +141,12 @@ __device__ __forceinline__ double src64(const ArpsCtx& c, const float* xf, const
 // Exact reference cost between the block at (i,j) of slice a1 and (y,x) of a2.
 template <int BS>
 __device__ double cost64(const ArpsCtx& c, int i, int j, int y, int x) {
+  const int nb = BS > 0 ? BS : c.bs;
   double v1 = 0.0, v2 = 0.0;
-  const double oo = 1.0 / (double)(BS * BS);
+  const double oo = 1.0 / (double)(nb * nb);
 #pragma unroll
-  for (int e = 0; e < BS * BS; ++e) {
-    const int r = e % BS, cc = e / BS;
+  for (int e = 0; e < nb * nb; ++e) {
+    const int r = e % nb, cc = e / nb;
     const size_t ka = (i + r) + (size_t)(j + cc) * c.S, kb = (y + r) + (size_t)(x + cc) * c.S;
     const double a = c.pa1 ? c.pa1[ka] : __ddiv_rn(src64(c, c.xa1, c.xa1d, ka), c.umax);
     const double b = c.pa2 ? c.pa2[kb] : __ddiv_rn(src64(c, c.xa2, c.xa2d, kb), c.umax);
@@ -206,7 +231,8 @@ template <int BS>
 __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, int& ox,
                           unsigned long long* nexact) {
   const int S = c.S, M = c.mw, Wd = 2 * M + 1;
-  const int n1 = S - BS + 1;
+  const int nb = BS > 0 ? BS : c.bs;
+  const int n1 = S - nb + 1;
   const int i = it % n1, j = it / n1;
   Block<BS> blk;
   blk.load(c, i, j);
@@ -263,7 +289,7 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
   for (int k = 0; k < nld; ++k) {
     if (k == 2 || step == 0) continue;
     const int vy = y + LD[k][1], hx = x + LD[k][0];
-    if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
+    if (hx < 0 || vy < 0 || hx + nb - 1 >= S || vy + nb - 1 >= S) continue;
     blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
     ev[k] = true;
     mark(LD[k][1], LD[k][0]);
@@ -286,7 +312,7 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
     for (int k = 0; k < 5; ++k) {
       if (k == 2) continue;
       const int vy = y + SD[k][1], hx = x + SD[k][0];
-      if (hx < 0 || vy < 0 || hx + BS - 1 >= S || vy + BS - 1 >= S) continue;
+      if (hx < 0 || vy < 0 || hx + nb - 1 >= S || vy + nb - 1 >= S) continue;
       if (hx < j - M || hx > j + M || vy < i - M || vy > i + M) continue;
       if (is_seen(vy - i, hx - j)) continue;
       blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
@@ -324,6 +350,7 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
   const float* xw = med ? d.zs : d.xs;
   const double* xd = med ? nullptr : d.x64;
   ArpsCtx c;
+  c.bs = g.bs;
   c.integer = med || d.int_input;
   c.umax = med ? wc.wnorm : wc.unorm;
   c.S = g.S;
@@ -379,7 +406,7 @@ cudaError_t launch_arps(const Problem& pb, const DeviceBuffers& d, cudaStream_t 
     case 6: k_arps<6><<<ga, threads, 0, s>>>(pb, d); break;
     case 7: k_arps<7><<<ga, threads, 0, s>>>(pb, d); break;
     case 8: k_arps<8><<<ga, threads, 0, s>>>(pb, d); break;
-    default: return cudaErrorInvalidValue;
+    default: k_arps<0><<<ga, threads, 0, s>>>(pb, d); break;  // sides 9..16
   }
   return cudaGetLastError();
 }

@@ -258,8 +258,8 @@ void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
     throw Fail(PGSVT_ERR_INVALID_ARG, "frames must be square (the reference's ARPS indexing, "
                                       "arps.hpp:186-187, assumes nrows == ncols)");
   if (nr > 32767) throw Fail(PGSVT_ERR_UNSUPPORTED, "frame side above 32767");
-  if (p.block_size < 2 || p.block_size > 8)
-    throw Fail(PGSVT_ERR_UNSUPPORTED, "block_size must be in [2, 8] in this build");
+  if (p.block_size < 2 || p.block_size > 16)
+    throw Fail(PGSVT_ERR_UNSUPPORTED, "block_size must be in [2, 16] in this build");
   if (p.block_size > nr) throw Fail(PGSVT_ERR_INVALID_ARG, "block_size larger than the frame");
   if (p.block_overlap < 1 || p.block_overlap > p.block_size)
     throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid patch_overlap parameter: must be in [1, block_size]");
@@ -479,8 +479,10 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   PGSVT_CK(cudaMemcpyAsync(hint.data(), fint, sizeof(int) * nimg, cudaMemcpyDeviceToHost, s));
   PGSVT_CK(cudaStreamSynchronize(s));
   stats.d2h += (sizeof(double) + sizeof(int)) * nimg;
-  int int_input = 1;  // ARPS integer mode for integer-valued inputs
+  int int_input = 1;  // ARPS integer mode for integer-valued inputs (arps.cu)
   for (int v : hint) int_input &= v;
+  if (g.M > 64)
+    for (double v : hmax) int_input &= (v <= 131072.0) ? 1 : 0;
   for (double v : hmax)
     if (v < 0) throw Fail(PGSVT_ERR_NONFINITE, "input holds negative, NaN or infinite values");
   // noise estimation tables per input frame (noise.cu)

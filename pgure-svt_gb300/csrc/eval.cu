@@ -338,7 +338,8 @@ constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x
 
 template <int BS, typename AccT>
 __global__ void __launch_bounds__(32 * 21) k_eval(Problem pb, DeviceBuffers d, int final_pass) {
-  constexpr int M = BS * BS;
+  const int nb = BS > 0 ? BS : pb.g.bs;  // BS == 0: any side (9..16)
+  const int M = nb * nb;
   constexpr int PB = kEvalPatches;  // patches per block
   const Geometry& g = pb.g;
   const int w = blockIdx.y;
@@ -428,12 +429,12 @@ __global__ void __launch_bounds__(32 * 21) k_eval(Problem pb, DeviceBuffers d, i
     x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
     x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
   }
-  const int th = y1 - y0 + BS, tw = x1 - x0 + BS;
+  const int th = y1 - y0 + nb, tw = x1 - x0 + nb;
   const bool use_tile = (y1 >= 0) && th * tw <= kTileMax;
   const float* U0 = d.U0 + (size_t)w * NC * M * NP;
   const float* V0 = d.V0 + (size_t)w * NC * g.nwin * NP;
   AccT* accw = (AccT*)d.acc;
-  constexpr int CH = M < 16 ? M : 16;  // rows rebuilt per pass (bounds registers)
+  constexpr int CH = (BS > 0 && BS * BS < 16) ? BS * BS : 16;  // rows rebuilt per pass
   for (int j = 0; j < nl; ++j) {
     AccT* acc = accw + (((size_t)w * pb.K + j) * g.nwin + k) * g.F();
 #pragma unroll 1
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(32 * 21) k_eval(Problem pb, DeviceBuffers d, i
           const int ee = e0 + e;
           const float v = col[e];
           if (ee >= M || v == 0.f) continue;
-          const int er = ee % BS, ec = ee / BS;
+          const int er = ee % nb, ec = ee / nb;
           if (use_tile && fabsf(v) <= kTileBound)
             atomicAdd(tile + (y[h] - y0 + er) + (x[h] - x0 + ec) * th, __float2int_rn(v * 1048576.f));
           else
@@ -626,7 +627,8 @@ void launch_k_eval_t(int bs, dim3 grid, int threads, size_t shm, cudaStream_t s,
     case 5: launch_k_eval_bs<5, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
     case 6: launch_k_eval_bs<6, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
     case 7: launch_k_eval_bs<7, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    default: launch_k_eval_bs<8, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 8: launch_k_eval_bs<8, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    default: launch_k_eval_bs<0, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
   }
 }
 

@@ -51,6 +51,7 @@ bool svd_supported(int bs, int nwin) {
 // order; all agree to FP32 rounding.  The autotuner (capi.cu) times them on the
 // caller's data and keeps the fastest.
 bool svd_variant_ok(int M, int v) {
+  if (M > 64) return v == 0;  // patch sides 9..16: the shared-memory form only
   if (v == 0 || v == 2) return true;
   return v == 1 && !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
 }
@@ -86,6 +87,10 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
     if (NC == 10) return run_pair<5, 8, 10>(pb, d, s);
     if (NC == 16) return run_pair<5, 8, 16>(pb, d, s);
     if (NC == 22) return run_pair<5, 8, 22>(pb, d, s);
+  } else if (M > 64) {  // bs 9..16: 8 rows x 32 lanes, columns in shared memory
+    if (NC == 10) return run_svd<8, 32, 10, true>(pb, d, s);
+    if (NC == 16) return run_svd<8, 32, 16, true>(pb, d, s);
+    if (NC == 22) return run_svd<8, 32, 22, true>(pb, d, s);
   } else {  // bs 7, 8
     if (alt) {
       if (NC == 10) return run_svd<2, 32, 10, false>(pb, d, s);

@@ -147,7 +147,9 @@ struct SvdSmem {
 // registers, (NC/2) * 2 * RPL floats
 template <int RPL, int NC, bool SM>
 constexpr int svd_minblocks() {
-  return SM ? ((NC / 2) * 2 * RPL <= 64 ? PGSVT_SVD_MINBLOCKS_SM : 2) : PGSVT_SVD_MINBLOCKS;
+  return SM ? ((NC / 2) * 2 * RPL <= 64 ? PGSVT_SVD_MINBLOCKS_SM
+                                        : ((NC / 2) * 2 * RPL <= 128 ? 2 : 1))
+            : PGSVT_SVD_MINBLOCKS;
 }
 
 template <int RPL, int LANES, int NC, bool SM = false>

@@ -156,3 +156,35 @@ def test_cli_end_to_end_matches_library(capi, pkg, tmp_path, hot):
     Y, _, _ = capi.denoise(X, p)
     ref = np.clip(Y, 0, 65535).astype(np.uint16)  # truncation, as the tool converts
     np.testing.assert_array_equal(out, np.transpose(ref, (2, 0, 1)))
+
+
+@pytest.mark.gpu
+def test_cli_reference_example_parameters(capi, pkg, tmp_path):
+    """The settings of the reference's examples/param_example.svt (16 x 16
+    patches, overlap 2, trajectory 15, fixed lambda 0.15, given noise, motion
+    estimation with the default median filter, seed 1) on a synthetic
+    sequence of the example's shape."""
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=6, side=64, nt=25)
+    frames = np.clip(np.round(noisy * 50), 0, 65535).astype(np.uint16)
+    write_tiff(tmp_path / "example.tif", np.transpose(frames, (2, 0, 1)), rows_per_strip=16)
+    (tmp_path / "p.svt").write_text(
+        "filename    : ./example.tif  # TIFF file to be denoised\n"
+        "start_frame : 1              # Start frame\n"
+        "end_frame   : 25             # End frame\n"
+        "patch_size            : 16    # Patch size in pixels (default = 4)\n"
+        "patch_overlap         : 2     # Patch overlap in pixels (default = 1)\n"
+        "trajectory_length     : 15    # must be odd\n"
+        "normalize             : false # no normalisation\n"
+        "noise_alpha           : 0.1\nnoise_mu              : 0.1\nnoise_sigma           : 0.1\n"
+        "optimize_pgure        : false\nlambda                : 0.15\n"
+        "motion_estimation     : true\n#median_filter        : 5\n"
+        "exponential_weighting : true\nrandom_seed           : 1\n")
+    r = run(tmp_path / "p.svt", tmp_path)
+    assert r.returncode == 0, r.stderr
+    out = read_tiff16(tmp_path / "example-CLEANED.tif")
+    p = capi.default_params(block_size=16, block_overlap=2, traj_length=15, median_size=5,
+                            optimize_pgure=0, lambda_=0.15, alpha=0.1, mu=0.1, sigma=0.1,
+                            random_seed=1, max_iter=1000)
+    Y, _, _ = capi.denoise(np.asfortranarray(frames), p)
+    np.testing.assert_array_equal(out, np.transpose(np.clip(Y, 0, 65535).astype(np.uint16),
+                                                    (2, 0, 1)))

@@ -273,3 +273,20 @@ def test_integer_input_arps_ties_match_oracle(capi, oracle, pkg):
                               lambda_=0.1, n_jobs=4)
     print("FP64 tie decisions:", st.arps_exact_steps)
     assert np.abs(Y - Y0).max() < 2e-5 * np.abs(Y0).max()
+
+
+@pytest.mark.parametrize("bs,T,ov", [(12, 9, 1), (16, 15, 2)])
+def test_large_patches_match_oracle(capi, oracle, pkg, bs, T, ov):
+    # patch sides 9..16 run the runtime-size ARPS and evaluation kernels and
+    # the 8 x 32-lane shared-memory SVD (256 rows for 16 x 16 patches)
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=12, side=40, nt=T + 3)
+    X = noisy.astype(np.float64)
+    fr = (T // 2, T // 2 + 3)
+    kw = dict(median_size=-1, optimize_pgure=0, lambda_=0.15, block_size=bs, block_overlap=ov,
+              traj_length=T, frame_begin=fr[0], frame_end=fr[1])
+    Y, _, _ = capi.denoise(X, capi.default_params(**kw))
+    Y0, _, _ = oracle.denoise(X, n_jobs=4, **kw)
+    f = slice(*fr)
+    err = np.abs(Y[:, :, f] - Y0[:, :, f]).max() / np.abs(Y0[:, :, f]).max()
+    print("max relative difference", err)
+    assert err < 1e-4
