@@ -8,8 +8,11 @@
 // Same parameter names, defaults and messages as PGURE-SVT.cpp:36-110, with
 // the reference's parameter-file grammar (ParseParameters, utils.hpp:55-92):
 // "key : value  # comment", tokens after the colon concatenated up to one
-// holding '#'.  As in the reference, `tolerance` is parsed but the run keeps
-// 1e-7 (PGURE-SVT.cpp:101-106 assigns it to a shadowing local), and the λ
+// holding '#'; a token that ends the line gets a trailing space (the
+// stream is at its end, so skipping whitespace fails), which makes a bare
+// "key : true" read as false, as in the reference.  As in the reference,
+// `tolerance` is parsed but the run keeps 1e-7 (PGURE-SVT.cpp:101-106
+// assigns it to a shadowing local), and the λ
 // start point passed is 0 when optimising.  TIFF I/O is built in (no
 // libtiff): baseline, uncompressed, 8- or 16-bit grayscale, strips, either
 // byte order; 8-bit frames are widened to 16 bits (the reference reads them

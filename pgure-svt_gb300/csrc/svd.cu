@@ -38,7 +38,7 @@ int svd_columns(int nwin) {
 
 bool svd_supported(int bs, int nwin) {
   // bs <= 4 clamps the window to bs*bs-1 <= 15 frames
-  return bs >= 2 && bs <= 8 && svd_columns(nwin) > 0;
+  return bs >= 2 && bs <= 16 && svd_columns(nwin) > 0;
 }
 
 // Kernel forms: rows per lane x lanes per patch covers bs*bs rows; the

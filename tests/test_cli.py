@@ -176,9 +176,9 @@ def test_cli_reference_example_parameters(capi, pkg, tmp_path):
         "trajectory_length     : 15    # must be odd\n"
         "normalize             : false # no normalisation\n"
         "noise_alpha           : 0.1\nnoise_mu              : 0.1\nnoise_sigma           : 0.1\n"
-        "optimize_pgure        : false\nlambda                : 0.15\n"
-        "motion_estimation     : true\n#median_filter        : 5\n"
-        "exponential_weighting : true\nrandom_seed           : 1\n")
+        "optimize_pgure        : false # fixed lambda\nlambda                : 0.15\n"
+        "motion_estimation     : true  # ARPS\n#median_filter        : 5\n"
+        "exponential_weighting : true  # weighting\nrandom_seed           : 1\n")
     r = run(tmp_path / "p.svt", tmp_path)
     assert r.returncode == 0, r.stderr
     out = read_tiff16(tmp_path / "example-CLEANED.tif")
@@ -188,3 +188,26 @@ def test_cli_reference_example_parameters(capi, pkg, tmp_path):
     Y, _, _ = capi.denoise(np.asfortranarray(frames), p)
     np.testing.assert_array_equal(out, np.transpose(np.clip(Y, 0, 65535).astype(np.uint16),
                                                     (2, 0, 1)))
+
+
+@pytest.mark.gpu
+def test_cli_boolean_without_trailing_comment_reads_false(capi, pkg, tmp_path):
+    """ParseParameters (utils.hpp:70-89) appends a space to a value that ends
+    its line, so StrToBool sees "true " and returns false; the reference's
+    example files put a comment after every value.  Reproduced: a bare
+    "motion_estimation : true" runs without motion estimation."""
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=7, side=32, nt=16)
+    frames = np.clip(np.round(noisy), 0, 65535).astype(np.uint16)
+    write_tiff(tmp_path / "s.tif", np.transpose(frames, (2, 0, 1)))
+    (tmp_path / "p.svt").write_text(
+        "filename : ./s.tif # in\nstart_frame : 1 # a\nend_frame : 16 # b\n"
+        "optimize_pgure : false # c\nlambda : 0.2 # d\nnoise_alpha : 0.1 # e\n"
+        "noise_mu : 0.1 # f\nnoise_sigma : 0.1 # g\nmotion_estimation : true\n")
+    r = run(tmp_path / "p.svt", tmp_path)
+    assert r.returncode == 0, r.stderr
+    out = read_tiff16(tmp_path / "s-CLEANED.tif")
+    kw = dict(median_size=5, optimize_pgure=0, lambda_=0.2, alpha=0.1, mu=0.1, sigma=0.1,
+              max_iter=1000)
+    Yoff, _, _ = capi.denoise(np.asfortranarray(frames), capi.default_params(motion_estimation=0, **kw))
+    ref = np.transpose(np.clip(Yoff, 0, 65535).astype(np.uint16), (2, 0, 1))
+    np.testing.assert_array_equal(out, ref)
