@@ -265,7 +265,10 @@ struct Estimator {
       case 1: {
         const int L = (int)std::floor(1.0 * (double)((size_t)nx * ny / means.size()));
         const uint32_t ie = (uint32_t)std::round(0.05 * L);
-        std::vector<double> a(rm.begin(), rm.begin() + ie + 1), b(rv.begin(), rv.begin() + ie + 1);
+        // the first ie + 1 leaves; clamped to the leaf count (the reference
+        // reads past its arrays when ie + 1 exceeds it)
+        const size_t ne = std::min<size_t>((size_t)ie + 1, rm.size());
+        std::vector<double> a(rm.begin(), rm.begin() + ne), b(rv.begin(), rv.begin() + ne);
         mu = (mu >= 0.0) ? mu : mode(a);
         const double dSi = mode(b);
         sigma = (sigma >= 0.0) ? sigma : std::sqrt(dSi);

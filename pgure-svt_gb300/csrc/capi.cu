@@ -282,8 +282,8 @@ void validate(const pgsvt_params& p, uint32_t nr, uint32_t nc, uint32_t nimg) {
                                         "(noise.hpp:216 has F-test values for 2^k blocks only); "
                                         "give alpha, mu and sigma");
     if (nr < 4) throw Fail(PGSVT_ERR_INVALID_ARG, "noise estimation needs frames of side >= 4");
-    if (p.noise_method != 3 && p.noise_method != 4)
-      throw Fail(PGSVT_ERR_UNSUPPORTED, "noise_method 1 and 2 are not built (3 and 4 are)");
+    if (p.noise_method < 1 || p.noise_method > 4)
+      throw Fail(PGSVT_ERR_INVALID_ARG, "noise_method must be 1, 2, 3 or 4");
   }
   if (!p.optimize_pgure && !(p.lambda >= 0))
     throw Fail(PGSVT_ERR_INVALID_ARG, "Invalid lambda1 parameter: must be >= 0 without optimisation");
@@ -586,6 +586,8 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     np.y = mem.arr<double>(chunk * per_w);
     np.key = mem.arr<unsigned long long>(chunk * per_w);
     np.hist = mem.arr<int>(chunk * (per_w + 1));
+    np.fkey = mem.arr<unsigned long long>(chunk * (per_w + 1));
+    np.fidx = mem.arr<int>(chunk * (per_w + 1));
     for (int k0 = 0; k0 < nwinds; k0 += chunk) {
       NoisePass npc = np;
       npc.nwindows = std::min(chunk, nwinds - k0);

@@ -7,9 +7,16 @@
 // robust mean (IRLS with Huber weights, noise.hpp:239-270) and a robust
 // variance of the Laplacian-filtered block (1.4826 MAD, noise.hpp:232-236,
 // 386-409), then an IRLS straight-line fit var = alpha * mean + beta over
-// all leaves of the window (noise.hpp:310-357).  Noise method 4 takes
-// mu = the smallest leaf mean, method 3 the mode of the leaf means; sigma =
-// sqrt(|beta + alpha * mu|).
+// all leaves of the window (noise.hpp:310-357).  The leaves taken in
+// ascending mean order, mu and sigma follow the method (noise.hpp:115-147):
+//   1  modes of the means and of the variances of the first
+//      round(0.05 * floor(Nx Ny / leaves)) + 1 leaves; sigma = sqrt(var mode)
+//   2  mu = mode of all means; v = mode of all variances;
+//      sigma = sqrt(max(v, beta + alpha v, 0))
+//   3  mu = mode of all means; sigma = sqrt(|beta + alpha mu|)
+//   4  mu = the smallest mean; sigma = sqrt(|beta + alpha mu|)
+// A mode (ComputeMode, noise.hpp:272-297) is the most frequent value of
+// round(v n / max v), ties going to the one met first in that order.
 //
 // GB300 mapping.  The split decisions and the leaf variances are
 // scale-equivariant, so they are computed once per input frame on the raw
@@ -35,7 +42,10 @@
 //                   the first one's results
 //   k_noise_fit     one cluster of 8 CTAs per window, all windows in one
 //                   launch (distributed shared memory for the sums and the
-//                   radix selections): the IRLS fit, mu, sigma
+//                   radix selections): the IRLS fit, mu, sigma; modes over
+//                   all leaves by a histogram of the n + 1 rounded values
+//                   with first-occurrence keys, method 1's few leaves by
+//                   a radix selection and the reference's O(n^2) count
 // All arithmetic is FP64.
 #include <cooperative_groups.h>
 
@@ -652,7 +662,10 @@ struct FitArgs {
   double* y;
   unsigned long long* key;
   int* hist;                 // [nwindows][nwin * maxNodes + 1]
+  unsigned long long* fkey;  // [nwindows][nwin * maxNodes + 1] first-occurrence keys
+  int* fidx;                 // [nwindows][nwin * maxNodes + 1]
   double* est;               // [nwindows][3] caller-side (alpha, mu, sigma)
+  int nx;                    // frame side
 };
 
 // WLSFit (noise.hpp:302-358) and the method's mu / sigma for every window:
@@ -734,36 +747,133 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_nois
   }
   mn = -cluster_max(cl, -mn, sm);
   mx = cluster_max(cl, mx, sm);
-  double mode = 0.0;
-  if (a.method == 3) {  // ComputeMode (noise.hpp:272-297) of the leaf means
-    int* h = a.hist + (size_t)w * (per + 1);
+  // mu and sigma by the noise method (noise.hpp:115-147)
+  int* h = a.hist + (size_t)w * (per + 1);
+  unsigned long long* fk = a.fkey + (size_t)w * (per + 1);
+  int* fi = a.fidx + (size_t)w * (per + 1);
+  __shared__ double s_res[2];
+  // ComputeMode (noise.hpp:272-297) of all N values v(i) taken in the
+  // means-sorted order: the most frequent rounded value round(v N / max),
+  // ties going to the value whose first occurrence (least (mean, index))
+  // comes first.  A histogram over the N + 1 rounded values.
+  auto mode_all = [&](auto v, double vmax, bool by_value) -> double {
     const double dyn = (double)N;
-    for (int i = lo + threadIdx.x; i < (rank + 1 == kCl ? N + 1 : hi); i += blockDim.x) h[i] = 0;
-    __threadfence();
-    cl.sync();
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      const double r = round(X[i] * dyn / mx);
-      atomicAdd(&h[(int)fmin(fmax(r, 0.0), dyn)], 1);
+    for (int t = lo + threadIdx.x; t < (rank + 1 == kCl ? N + 1 : hi); t += blockDim.x) {
+      h[t] = 0;
+      fk[t] = ~0ull;
+      fi[t] = 0x7fffffff;
     }
     __threadfence();
     cl.sync();
-    __shared__ double s_mode;
-    if (threadIdx.x == 0) {  // most frequent rounded value; ties: the smallest
+    auto bin = [&](int t) { return (int)fmin(fmax(round(v(t) * dyn / vmax), 0.0), dyn); };
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+      const int b = bin(t);
+      atomicAdd(&h[b], 1);
+      if (!by_value) atomicMin(&fk[b], okey(X[t]));
+    }
+    __threadfence();
+    cl.sync();
+    if (!by_value) {
+      for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+        const int b = bin(t);
+        if (okey(X[t]) == fk[b]) atomicMin(&fi[b], t);
+      }
+      __threadfence();
+      cl.sync();
+    }
+    if (threadIdx.x == 0) {
       int best = 0, bc = -1;
-      for (int i = 0; i <= N; ++i)
-        if (h[i] > bc) {
-          bc = h[i];
-          best = i;
+      for (int t = 0; t <= N; ++t) {
+        // by value (sorted values): the smallest of the most frequent;
+        // else the one whose first occurrence comes first
+        const bool better = h[t] > bc ||
+                            (!by_value && h[t] == bc && bc > 0 &&
+                             (fk[t] < fk[best] || (fk[t] == fk[best] && fi[t] < fi[best])));
+        if (better) {
+          bc = h[t];
+          best = t;
         }
-      s_mode = (double)best * mx / dyn;
+      }
+      s_res[0] = (double)best * vmax / dyn;
     }
     __syncthreads();
-    mode = s_mode;
+    const double r = s_res[0];
+    cl.sync();  // the scratch is reused by the next call
+    return r;
+  };
+  double mu = a.mu_c, sigma = a.sigma_c;
+  if (a.method == 1) {
+    // the K = round(0.05 L) + 1 leaves of least mean (L = Nx Ny / N, integer
+    // division), modes of their means and of their variances; K is clamped to
+    // N (beyond N the reference reads past its arrays)
+    const int L = (int)(((long long)a.nx * a.nx) / N);
+    const int K = min(N, (int)llround(0.05 * L) + 1);
+    unsigned long long tk, tk2;
+    cluster_select2(cl, [&](int t) { return okey(X[t]); }, lo, hi, K - 1, K - 1, sm, tk, tk2);
+    int* cnt = fi;  // count of candidates, then their indices
+    if (rank == 0 && threadIdx.x == 0) cnt[0] = 0;
+    __threadfence();
+    cl.sync();
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x)
+      if (okey(X[t]) <= tk) {
+        const int slot = atomicAdd(&cnt[0], 1);
+        if (slot < (int)per) cnt[1 + slot] = t;
+      }
+    __threadfence();
+    cl.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+      const int nc = min(cnt[0], (int)per);
+      int* idx = cnt + 1;
+      for (int p = 1; p < nc; ++p)  // order by (mean, index)
+        for (int q = p; q > 0; --q) {
+          const unsigned long long ka = okey(X[idx[q - 1]]), kb = okey(X[idx[q]]);
+          if (ka < kb || (ka == kb && idx[q - 1] < idx[q])) break;
+          const int t = idx[q];
+          idx[q] = idx[q - 1];
+          idx[q - 1] = t;
+        }
+      auto mode_small = [&](auto v, int n) {  // ComputeMode as written, O(n^2)
+        double M = v(0);
+        for (int t = 1; t < n; ++t) M = fmax(M, v(t));
+        const double dyn = (double)n;
+        int maxCount = 0;
+        double maxValue = 0.0;
+        for (int t = 0; t < n; ++t) {
+          const double at = round(v(t) * dyn / M);
+          int c = 0;
+          for (int u = 0; u < n; ++u) c += round(v(u) * dyn / M) == at;
+          if (c > maxCount) {
+            maxCount = c;
+            maxValue = at;
+          }
+        }
+        return maxValue * M / dyn;
+      };
+      const int n = min(K, nc);
+      s_res[0] = mode_small([&](int t) { return X[idx[t]]; }, n);
+      s_res[1] = mode_small([&](int t) { return Y[idx[t]]; }, n);
+    }
+    __syncthreads();
+    if (mu < 0) mu = s_res[0];
+    if (sigma < 0) sigma = sqrt(s_res[1]);
+  } else if (a.method == 2) {
+    double ymx = -1e300;
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) ymx = fmax(ymx, Y[t]);
+    ymx = cluster_max(cl, ymx, sm);
+    const double mmode = mode_all([&](int t) { return X[t]; }, mx, true);
+    const double dSi = mode_all([&](int t) { return Y[t]; }, ymx, false);
+    if (mu < 0) mu = mmode;
+    if (sigma < 0) sigma = sqrt(fmax(dSi, fmax(p1 + p0 * dSi, 0.0)));
+  } else if (a.method == 3) {
+    const double mmode = mode_all([&](int t) { return X[t]; }, mx, true);
+    if (mu < 0) mu = mmode;
+    if (sigma < 0) sigma = sqrt(fabs(p1 + p0 * mu));
+  } else {
+    if (mu < 0) mu = mn;
+    if (sigma < 0) sigma = sqrt(fabs(p1 + p0 * mu));
   }
   if (rank == 0 && threadIdx.x == 0) {
     const double alpha = a.alpha_c >= 0 ? a.alpha_c : p0;
-    const double mu = a.mu_c >= 0 ? a.mu_c : (a.method == 3 ? mode : mn);
-    const double sigma = a.sigma_c >= 0 ? a.sigma_c : sqrt(fabs(p1 + p0 * mu));
     a.est[(size_t)w * 3] = alpha;
     a.est[(size_t)w * 3 + 1] = mu;
     a.est[(size_t)w * 3 + 2] = sigma;
@@ -833,7 +943,7 @@ cudaError_t launch_noise_pass(const NoiseFrames& nf, const NoisePass& np, const 
   }
   FitArgs fa{nf.nleaf, nf.dup, nf.stats, np.mean, np.win_pair, np.win_s0, np.win_norm,
              nf.maxNodes, np.nwin, np.method, np.alpha_c, np.mu_c, np.sigma_c, np.x, np.y,
-             np.key, np.hist, np.est};
+             np.key, np.hist, np.fkey, np.fidx, np.est, S};
   k_noise_fit<<<dim3(kCl, np.nwindows), kClThreads, 0, s>>>(fa);
   return cudaGetLastError();
 }

@@ -236,6 +236,8 @@ struct NoisePass {
   double* y;
   unsigned long long* key;
   int* hist;                 // [nwindows][nwin * maxNodes + 1]
+  unsigned long long* fkey;  // [nwindows][nwin * maxNodes + 1] mode scratch
+  int* fidx;                 // [nwindows][nwin * maxNodes + 1]
   double* est;               // [nwindows][3] (alpha, mu, sigma), caller-side
 };
 int noise_levels(int S);

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-@pytest.mark.parametrize("method", [3, 4])
+@pytest.mark.parametrize("method", [1, 2, 3, 4])
 def test_estimates_match_frozen_oracle(capi, method):
     """One window per case: a sequence of exactly T frames has one window,
     and its frames are the frozen normalised window (max 1)."""
@@ -85,5 +85,5 @@ def test_estimation_limits(capi, pkg):
     assert e.value.code == capi.ERR_UNSUPPORTED
     X = np.ones((32, 32, 16), np.float32)
     with pytest.raises(pkg.PgsvtError) as e:
-        capi.denoise(X, capi.default_params(median_size=0, noise_method=1))
-    assert e.value.code == capi.ERR_UNSUPPORTED
+        capi.denoise(X, capi.default_params(median_size=0, noise_method=5))
+    assert e.value.code == capi.ERR_INVALID_ARG
