@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=0,
                     help="also time pgsvt_denoise_batch on this many uneven sequences")
     ap.add_argument("--autotune", type=int, default=1,
-                    help="SVD kernel form: 1 tuned (default), 0 registers, 3 shared memory")
+                    help="SVD kernel form: 1 tuned (default), 0 registers, 2 more lanes, "
+                    "3 shared memory, 4 eight rows per lane")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-stride", type=int, default=0, help="patch stride of the CPU sample")
     return ap.parse_args()

@@ -117,7 +117,8 @@ typedef struct {
                                0: the default shape; 2: more lanes per
                                patch where the patch size has that form;
                                3: the default shape with its columns in
-                               shared memory                                 */
+                               shared memory; 4: 8 rows per lane (patch
+                               sides <= 4 and 7..8, windows <= 16)           */
 } pgsvt_params;
 
 /* Optional per-frame outputs of pgsvt_denoise_ex / pgsvt_denoise_device_ex

@@ -66,7 +66,7 @@ struct Block {
   // m <= 64, or umax <= 2^17 and m <= 256 (the host enables the mode only
   // then): comparing D decides exactly as the reference does, except for
   // equal D.
-  __device__ double ssd(const ArpsCtx& c, int y, int x) const {
+  __device__ unsigned long long ssd(const ArpsCtx& c, int y, int x) const {
     const int nb = BS > 0 ? BS : c.bs;
     unsigned long long acc = 0ull;
 #pragma unroll
@@ -78,7 +78,7 @@ struct Block {
         const long long d = a - b;
         acc += (unsigned long long)(d * d);
       }
-    return (double)acc;  // < 2^53: exact
+    return acc;
   }
 
   // the candidate block at (y, x) equals the one at (y2, x2), element by element
@@ -95,14 +95,15 @@ struct Block {
   }
 
   // cost of the candidate at (y, x): FP32 with an error bound, or exact D
-  __device__ void cost(const ArpsCtx& c, int y, int x, float& cf, float& err, double& cd) const {
+  __device__ void cost(const ArpsCtx& c, int y, int x, float& cf, float& err,
+                       unsigned long long& cd) const {
     if (c.integer) {
       cd = ssd(c, y, x);
       cf = 0.f;
       err = 0.f;
     } else {
       cost32(c, y, x, cf, err);
-      cd = 0.0;
+      cd = 0ull;
     }
   }
 
@@ -138,67 +139,126 @@ __device__ __forceinline__ double src64(const ArpsCtx& c, const float* xf, const
   return xd ? xd[idx] : (double)xf[idx];
 }
 
-// Exact reference cost between the block at (i,j) of slice a1 and (y,x) of a2.
+// Per-warp scratch of the exact (FP64) decisions.
 template <int BS>
-__device__ double cost64(const ArpsCtx& c, int i, int j, int y, int x) {
+struct ArpsWarp {
+  static constexpr int kSq = BS > 0 ? 128 : 256;  // squared differences per pass
+  double sq[kSq];
+  double cst[6];      // exact cost per slot
+  uint32_t pos[6];    // candidate (y, x) per slot, 16 bits each
+  int bi, bj;         // reference block
+  unsigned em;        // slots to evaluate
+};
+
+__device__ __forceinline__ int nth_slot(unsigned em, int n) {
+  for (int k = 0; k < 6; ++k)
+    if ((em >> k) & 1u) {
+      if (n == 0) return k;
+      --n;
+    }
+  return 0;
+}
+
+// Exact reference costs (arps.hpp:148-151 as the reference evaluates them:
+// FP64 x/umax, FP64 squares, Armadillo's two-accumulator accu(), no fused
+// multiply-add) of the slots ws.em for the block at (ws.bi, ws.bj), by the
+// whole warp: the squared differences are spread over the lanes, and the
+// even- and odd-element accumulators of every slot are summed in element
+// order by two lanes.  The FP64 pipe runs a warp instruction at a fraction of
+// the FP32 rate whatever its active lanes, so one lane's exact step costs about
+// a tenth of the FP64 instructions of a per-thread evaluation.
+template <int BS>
+__device__ void warp_cost64(const ArpsCtx& c, ArpsWarp<BS>& ws) {
+  const int lane = threadIdx.x & 31;
   const int nb = BS > 0 ? BS : c.bs;
-  double v1 = 0.0, v2 = 0.0;
-  const double oo = 1.0 / (double)(nb * nb);
-#pragma unroll
-  for (int e = 0; e < nb * nb; ++e) {
-    const int r = e % nb, cc = e / nb;
-    const size_t ka = (i + r) + (size_t)(j + cc) * c.S, kb = (y + r) + (size_t)(x + cc) * c.S;
-    const double a = c.pa1 ? c.pa1[ka] : __ddiv_rn(src64(c, c.xa1, c.xa1d, ka), c.umax);
-    const double b = c.pa2 ? c.pa2[kb] : __ddiv_rn(src64(c, c.xa2, c.xa2d, kb), c.umax);
-    const double d = __dsub_rn(a, b);
-    const double sq = __dmul_rn(d, d);
-    if (e & 1) v2 = __dadd_rn(v2, sq);
-    else v1 = __dadd_rn(v1, sq);
+  const int m = nb * nb;
+  const double oo = 1.0 / (double)m;
+  const unsigned em = ws.em;
+  const int nc = __popc(em);
+  const int per = m >= ArpsWarp<BS>::kSq ? 1 : ArpsWarp<BS>::kSq / m;
+  for (int c0 = 0; c0 < nc; c0 += per) {
+    const int cn = min(per, nc - c0);
+    for (int t = lane; t < cn * m; t += 32) {
+      const int k = nth_slot(em, c0 + t / m);
+      const int e = t % m, r = e % nb, cc = e / nb;
+      const uint32_t pk = ws.pos[k];
+      const int py = (int)(pk & 0xffffu), px = (int)(pk >> 16);
+      const size_t ka = (ws.bi + r) + (size_t)(ws.bj + cc) * c.S;
+      const size_t kb = (py + r) + (size_t)(px + cc) * c.S;
+      const double a = c.pa1 ? c.pa1[ka] : __ddiv_rn(src64(c, c.xa1, c.xa1d, ka), c.umax);
+      const double b = c.pa2 ? c.pa2[kb] : __ddiv_rn(src64(c, c.xa2, c.xa2d, kb), c.umax);
+      const double d = __dsub_rn(a, b);
+      ws.sq[t] = __dmul_rn(d, d);
+    }
+    __syncwarp();
+    double v = 0.0;
+    if (lane < 2 * cn) {
+      const double* q = ws.sq + (lane >> 1) * m;
+      for (int e = lane & 1; e < m; e += 2) v = __dadd_rn(v, q[e]);
+    }
+    const double v2 = __shfl_down_sync(0xffffffffu, v, 1);
+    if (lane < 2 * cn && !(lane & 1))
+      ws.cst[nth_slot(em, c0 + (lane >> 1))] = __dmul_rn(__dadd_rn(v, v2), oo);
+    __syncwarp();
   }
-  return __dmul_rn(__dadd_rn(v1, v2), oo);
+}
+
+// The slot chosen from the exact costs of the slots em: integer mode, the
+// first of the least cost among the tied slots; otherwise the first index of
+// the minimum over every evaluated slot (unevaluated ones count as 1e9).
+__device__ int resolve_exact(bool integer, const double* cst, unsigned em, int nslot) {
+  if (integer) {
+    int kb = -1;
+    double mm = 0.0;
+    for (int k = 0; k < nslot; ++k) {
+      if (!((em >> k) & 1u)) continue;
+      if (kb < 0 || cst[k] < mm) {
+        mm = cst[k];
+        kb = k;
+      }
+    }
+    return kb;
+  }
+  double c64[6];
+  for (int k = 0; k < nslot; ++k) c64[k] = ((em >> k) & 1u) ? cst[k] : 1e9;
+  double mm = c64[0];
+  for (int k = 1; k < nslot; ++k) mm = fmin(mm, c64[k]);
+  for (int k = 0; k < nslot; ++k)
+    if (c64[k] == mm) return k;
+  return 2;
 }
 
 // Integer mode: first index of the least D; equal D decided as the
 // reference does: identical candidate blocks have identical FP64 costs (the
-// first one wins), otherwise the FP64 costs of the tied candidates decide.
+// first one wins), otherwise the FP64 costs of the tied candidates decide
+// (returns -1 with those slots in em).
 template <int BS>
-__device__ int pick_int(const ArpsCtx& c, const Block<BS>& blk, const double* cd, const bool* ev,
-                        const int (*off)[2], int nslot, int i, int j, int y, int x,
-                        unsigned long long* nexact) {
+__device__ int decide_int(const ArpsCtx& c, const Block<BS>& blk, const unsigned long long* cd,
+                          const bool* ev, const int (*off)[2], int nslot, int y, int x,
+                          unsigned& em) {
   int ks = 2;
-  double best = cd[2];
+  unsigned long long best = cd[2];
   for (int k = 0; k < nslot; ++k)
     if (ev[k] && (cd[k] < best || (cd[k] == best && k < ks))) {
       best = cd[k];
       ks = k;
     }
-  bool tie = false, distinct = false;
+  unsigned tied = 1u << ks;
+  bool distinct = false;
   for (int k = 0; k < nslot; ++k) {
     if (!ev[k] || k == ks || cd[k] != best) continue;
-    tie = true;
+    tied |= 1u << k;
     if (!blk.same(c, y + off[k][1], x + off[k][0], y + off[ks][1], x + off[ks][0])) distinct = true;
   }
-  if (!tie || !distinct) return ks;
-  atomicAdd(nexact, 1ull);
-  int kb = -1;
-  double m = 0.0;
-  for (int k = 0; k < nslot; ++k) {
-    if (!ev[k] || cd[k] != best) continue;
-    const double v = cost64<BS>(c, i, j, y + off[k][1], x + off[k][0]);
-    if (kb < 0 || v < m) {
-      m = v;
-      kb = k;
-    }
-  }
-  return kb;
+  if (!distinct) return ks;
+  em = tied;
+  return -1;
 }
 
-// First index of the minimum among evaluated slots; recomputes in FP64 when
-// the FP32 decision is not certain.  off[k] = (dx, dy) relative to (y, x).
-template <int BS>
-__device__ int pick(const ArpsCtx& c, const float* cs, const float* es, const bool* ev,
-                    const int (*off)[2], int nslot, int i, int j, int y, int x,
-                    unsigned long long* nexact) {
+// First index of the minimum among evaluated slots when the FP32 decision is
+// certain under the error bounds; else -1 with every evaluated slot in em.
+__device__ int decide_f32(const float* cs, const float* es, const bool* ev, int nslot,
+                          unsigned& em) {
   int ks = 2;
   float best = cs[2];
   for (int k = 0; k < nslot; ++k)
@@ -214,22 +274,21 @@ __device__ int pick(const ArpsCtx& c, const float* cs, const float* es, const bo
     if (k < ks ? !(lo > hi) : !(lo >= hi)) certain = false;
   }
   if (certain) return ks;
-  atomicAdd(nexact, 1ull);
-  double c64[6];
+  em = 0u;
   for (int k = 0; k < nslot; ++k)
-    c64[k] = ev[k] ? cost64<BS>(c, i, j, y + off[k][1], x + off[k][0]) : 1e9;
-  double m = c64[0];
-  for (int k = 1; k < nslot; ++k) m = fmin(m, c64[k]);
-  for (int k = 0; k < nslot; ++k)
-    if (c64[k] == m) return k;
-  return 2;
+    if (ev[k]) em |= 1u << k;
+  return -1;
 }
 
 // ARPSMotionEstimation (arps.hpp:153-375) for one position of one frame pair.
 // (my, mx) holds the predictor slot on entry and the new motion on exit.
+// The lanes of a warp step through the diamond searches together (a lane
+// whose search ended, or that holds no position, idles), so that the exact
+// decisions any of them needs are taken by the whole warp.
 template <int BS>
-__device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, int& ox,
-                          unsigned long long* nexact) {
+__device__ void arps_pair(const ArpsCtx& c, bool live, int it, int& my, int& mx, int& oy,
+                          int& ox, ArpsWarp<BS>& ws, unsigned& nexact) {
+  const int lane = threadIdx.x & 31;
   const int S = c.S, M = c.mw, Wd = 2 * M + 1;
   const int nb = BS > 0 ? BS : c.bs;
   const int n1 = S - nb + 1;
@@ -250,15 +309,11 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
   };
   int x = j, y = i;
   float cs[6], es[6];
-  double cd[6];
+  unsigned long long cd[6];
   bool ev[6];
   float curC, curE;
-  double curD;
+  unsigned long long curD;
   blk.cost(c, i, j, curC, curE, curD);
-  auto choose = [&](const int (*off)[2], int nslot) {
-    return c.integer ? pick_int<BS>(c, blk, cd, ev, off, nslot, i, j, y, x, nexact)
-                     : pick<BS>(c, cs, es, ev, off, nslot, i, j, y, x, nexact);
-  };
   mark(0, 0);
   int step, nld;
   int LD[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
@@ -280,52 +335,77 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
   LD[1][0] = -step;
   LD[3][0] = step;
   LD[4][1] = step;
-  // LDSP (arps.hpp:247-294)
+  // LDSP candidates (arps.hpp:247-287)
   for (int k = 0; k < 6; ++k) ev[k] = false;
   ev[2] = true;
   cs[2] = curC;
   es[2] = curE;
   cd[2] = curD;
-  for (int k = 0; k < nld; ++k) {
-    if (k == 2 || step == 0) continue;
-    const int vy = y + LD[k][1], hx = x + LD[k][0];
-    if (hx < 0 || vy < 0 || hx + nb - 1 >= S || vy + nb - 1 >= S) continue;
-    blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
-    ev[k] = true;
-    mark(LD[k][1], LD[k][0]);
-  }
-  int ks = choose(LD, 6);
-  x += LD[ks][0];
-  y += LD[ks][1];
-  curC = cs[ks];
-  curE = es[ks];
-  curD = cd[ks];
-  // SDSP (arps.hpp:299-368); every move enters an unvisited cell, so the loop
-  // ends within Wd*Wd iterations.
-  const int SD[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
-  for (int n = 0; n < Wd * Wd + 1; ++n) {
-    for (int k = 0; k < 6; ++k) ev[k] = false;
-    ev[2] = true;
-    cs[2] = curC;
-    es[2] = curE;
-    cd[2] = curD;
-    for (int k = 0; k < 5; ++k) {
-      if (k == 2) continue;
-      const int vy = y + SD[k][1], hx = x + SD[k][0];
+  if (live)
+    for (int k = 0; k < nld; ++k) {
+      if (k == 2 || step == 0) continue;
+      const int vy = y + LD[k][1], hx = x + LD[k][0];
       if (hx < 0 || vy < 0 || hx + nb - 1 >= S || vy + nb - 1 >= S) continue;
-      if (hx < j - M || hx > j + M || vy < i - M || vy > i + M) continue;
-      if (is_seen(vy - i, hx - j)) continue;
       blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
       ev[k] = true;
-      mark(vy - i, hx - j);
+      mark(LD[k][1], LD[k][0]);
     }
-    ks = choose(SD, 5);
-    if (ks == 2) break;
-    x += SD[ks][0];
-    y += SD[ks][1];
-    curC = cs[ks];
-    curE = es[ks];
-    curD = cd[ks];
+  // step 0 decides the LDSP (arps.hpp:289-294), steps 1.. the SDSP
+  // (arps.hpp:299-368); every SDSP move enters an unvisited cell, so a search
+  // ends within Wd*Wd moves.
+  const int SD[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
+  bool done = !live;
+  for (int n = 0; n <= Wd * Wd + 1; ++n) {
+    const int (*off)[2] = (n == 0) ? LD : SD;
+    const int nslot = (n == 0) ? 6 : 5;
+    if (n > 0 && !done) {
+      for (int k = 0; k < 6; ++k) ev[k] = false;
+      ev[2] = true;
+      cs[2] = curC;
+      es[2] = curE;
+      cd[2] = curD;
+      for (int k = 0; k < 5; ++k) {
+        if (k == 2) continue;
+        const int vy = y + SD[k][1], hx = x + SD[k][0];
+        if (hx < 0 || vy < 0 || hx + nb - 1 >= S || vy + nb - 1 >= S) continue;
+        if (hx < j - M || hx > j + M || vy < i - M || vy > i + M) continue;
+        if (is_seen(vy - i, hx - j)) continue;
+        blk.cost(c, vy, hx, cs[k], es[k], cd[k]);
+        ev[k] = true;
+        mark(vy - i, hx - j);
+      }
+    }
+    int ks = 2;
+    unsigned em = 0u;
+    if (!done)
+      ks = c.integer ? decide_int<BS>(c, blk, cd, ev, off, nslot, y, x, em)
+                     : decide_f32(cs, es, ev, nslot, em);
+    for (unsigned want = __ballot_sync(0xffffffffu, em != 0u); want; want &= want - 1u) {
+      const int L = __ffs(want) - 1;
+      if (lane == L) {
+        for (int k = 0; k < nslot; ++k)
+          ws.pos[k] = ((uint32_t)(y + off[k][1]) & 0xffffu) | ((uint32_t)(x + off[k][0]) << 16);
+        ws.bi = i;
+        ws.bj = j;
+        ws.em = em;
+      }
+      __syncwarp();
+      warp_cost64<BS>(c, ws);
+      if (lane == L) {
+        ks = resolve_exact(c.integer, ws.cst, em, nslot);
+        ++nexact;
+      }
+      __syncwarp();
+    }
+    if (!done) {
+      x += off[ks][0];
+      y += off[ks][1];
+      curC = cs[ks];
+      curE = es[ks];
+      curD = cd[ks];
+      if (n > 0 && ks == 2) done = true;
+    }
+    if (!__any_sync(0xffffffffu, !done)) break;
   }
   my = y - i;
   mx = x - j;
@@ -334,13 +414,16 @@ __device__ void arps_pair(const ArpsCtx& c, int it, int& my, int& mx, int& oy, i
 }
 
 template <int BS>
-__global__ void k_arps(Problem pb, DeviceBuffers d) {
+__global__ void __launch_bounds__(128) k_arps(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
-  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  const int it0 = blockIdx.x * blockDim.x + threadIdx.x;
   const int ch = blockIdx.y, w = blockIdx.z;
-  if (it >= g.P) return;
   const ArpsChain cn = d.chains[w * d.nchains + ch];
-  if (cn.npairs == 0) return;
+  if (cn.npairs == 0) return;  // uniform over the block
+  const bool live = it0 < g.P;
+  const int it = live ? it0 : 0;
+  __shared__ ArpsWarp<BS> wsh[4];
+  ArpsWarp<BS>& ws = wsh[threadIdx.x >> 5];
   const WinConst& wc = d.wc[w];
   const size_t F = g.F();
   // ARPS input: the median-filtered window when the pre-filter is on
@@ -356,6 +439,7 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
   c.S = g.S;
   c.mw = g.mw;
   int my = 0, mx = 0;
+  unsigned nexact = 0u;
   for (int q = 0; q < cn.npairs; ++q) {
     const int a1 = cn.a1[q], a2 = cn.a2[q];
     c.fa1 = fw + ((size_t)w * g.nwin + a1) * F;
@@ -367,9 +451,11 @@ __global__ void k_arps(Problem pb, DeviceBuffers d) {
     c.pa1 = d.w64 ? d.w64 + ((size_t)w * g.nwin + a1) * F : nullptr;
     c.pa2 = d.w64 ? d.w64 + ((size_t)w * g.nwin + a2) * F : nullptr;
     int oy, ox;
-    arps_pair<BS>(c, it, my, mx, oy, ox, d.counters);
-    d.pos[((size_t)w * g.nwin + a2) * g.P + it] = (uint32_t)oy | ((uint32_t)ox << 16);
+    arps_pair<BS>(c, live, it, my, mx, oy, ox, ws, nexact);
+    if (live) d.pos[((size_t)w * g.nwin + a2) * g.P + it] = (uint32_t)oy | ((uint32_t)ox << 16);
   }
+  for (int o = 16; o > 0; o >>= 1) nexact += __shfl_xor_sync(0xffffffffu, nexact, o);
+  if ((threadIdx.x & 31) == 0 && nexact) atomicAdd(d.counters, (unsigned long long)nexact);
 }
 
 // Reference slice (always) and, without motion estimation, the other slices:

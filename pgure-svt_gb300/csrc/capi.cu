@@ -403,7 +403,7 @@ std::map<std::pair<int, int>, int> g_tuned;
 // of two runs each) and keep the fastest; leaves the outputs of the chosen
 // shape in place.
 int tune_svd(Problem& pb, const DeviceBuffers& d, cudaStream_t s, Stats& stats) {
-  const int nv = 3;
+  const int nv = kSvdVariants;
   cudaEvent_t e0, e1;
   PGSVT_CK(cudaEventCreate(&e0));
   PGSVT_CK(cudaEventCreate(&e1));
@@ -411,7 +411,7 @@ int tune_svd(Problem& pb, const DeviceBuffers& d, cudaStream_t s, Stats& stats) 
   int best = 0, last = 0;
   float best_ms = 0.f;
   for (int v = 0; v < nv; ++v) {
-    if (!svd_variant_ok(pb.g.M, v)) continue;
+    if (!svd_variant_ok(pb.g.M, pb.g.NC, v)) continue;
     pb.svd_variant = v;
     float ms = 0.f;
     for (int rep = 0; rep < 2; ++rep) {
@@ -450,14 +450,14 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   // SVD kernel shape: tuned once per process and geometry when asked
   const std::pair<int, int> tkey(pb.g.M, pb.g.NC);
   bool tune = false;
-  if (p.autotune == 2 || p.autotune == 3) {  // forced: more lanes per patch / shared memory
-    const int v = p.autotune == 2 ? 1 : 2;
-    pb.svd_variant = svd_variant_ok(pb.g.M, v) ? v : 0;
+  if (p.autotune >= 2) {  // forced: shape autotune - 1 where the patch size has it
+    const int v = (int)p.autotune - 1;
+    pb.svd_variant = svd_variant_ok(pb.g.M, pb.g.NC, v) ? v : 0;
   } else if (p.autotune) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(tkey);
     if (it != g_tuned.end()) pb.svd_variant = it->second;
-    else tune = svd_variants(pb.g.M) > 1;
+    else tune = svd_variants(pb.g.M, pb.g.NC) > 1;
   }
   stats.svd_variant = pb.svd_variant;
   const Geometry& g = pb.g;

@@ -285,8 +285,9 @@ void set_last_error(const std::string& m);
 int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
 int svd_columns(int nwin);
-int svd_variants(int M);
-bool svd_variant_ok(int M, int v);
+constexpr int kSvdVariants = 4;
+int svd_variants(int M, int NC);
+bool svd_variant_ok(int M, int NC, int v);
 bool svd_supported(int bs, int nwin);
 
 }  // namespace pgsvt

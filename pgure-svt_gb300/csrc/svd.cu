@@ -47,15 +47,23 @@ bool svd_supported(int bs, int nwin) {
 // (moved one position per round), variant 1 spreads a patch over more lanes
 // (fewer registers per lane, more shuffles per inner product), variant 2 is the
 // default shape with the columns in shared memory (addressed by the round's
-// schedule, no moves).  Variants 0 and 2 apply the same rotations in the same
-// order; all agree to FP32 rounding.  The autotuner (capi.cu) times them on the
-// caller's data and keeps the fastest.
-bool svd_variant_ok(int M, int v) {
+// schedule, no moves), variant 3 holds 8 rows per lane in fewer lanes (the
+// per-pair rotation arithmetic, replicated in every lane of a patch, is shared
+// by twice the rows; 2 resident blocks per SM instead of 3).  Variants 0 and 2
+// apply the same rotations in the same order; all agree to FP32 rounding.  The
+// autotuner (capi.cu) times them on the caller's data and keeps the fastest.
+bool svd_variant_ok(int M, int NC, int v) {
   if (M > 64) return v == 0;  // patch sides 9..16: the shared-memory form only
   if (v == 0 || v == 2) return true;
-  return v == 1 && !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
+  if (v == 1) return !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
+  if (v == 3) return NC <= 16 && (M <= 16 || M > 40);  // 8 x 2 and 8 x 8 lanes
+  return false;
 }
-int svd_variants(int M) { return svd_variant_ok(M, 1) ? 3 : 2; }
+int svd_variants(int M, int NC) {
+  int n = 0;
+  for (int v = 0; v < kSvdVariants; ++v) n += svd_variant_ok(M, NC, v);
+  return n;
+}
 
 template <int RPL, int LANES, int NC>
 cudaError_t run_pair(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
@@ -67,6 +75,15 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
   using namespace svdk;
   const int M = pb.g.M, NC = pb.g.NC;
   const bool alt = pb.svd_variant == 1;
+  if (pb.svd_variant == 3 && NC <= 16) {  // 8 rows per lane
+    if (M <= 16) {
+      if (NC == 10) return run_svd<8, 2, 10, false>(pb, d, s);
+      if (NC == 16) return run_svd<8, 2, 16, false>(pb, d, s);
+    } else if (M > 40 && M <= 64) {
+      if (NC == 10) return run_svd<8, 8, 10, false>(pb, d, s);
+      if (NC == 16) return run_svd<8, 8, 16, false>(pb, d, s);
+    }
+  }
   if (M <= 16) {  // bs 2..4
     if (alt) {
       if (NC == 10) return run_svd<2, 8, 10, false>(pb, d, s);

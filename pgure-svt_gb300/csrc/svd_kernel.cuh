@@ -18,15 +18,61 @@ constexpr float kDegen = 1e-3f;   // |a_i|^2 and |a_j|^2 within 0.1%: near-degen
 // paired; after each round positions 0..NC-2 shift by one.  NC-1 rounds pair
 // every two columns once and bring every column back to its position.
 
-template <int RPL, int NC>
-__device__ __forceinline__ void shift_round(float (&A)[RPL][NC], float (&nrm)[NC]) {
-#pragma unroll
-  for (int r = 0; r < RPL; ++r) {
-    const float t = A[r][0];
-#pragma unroll
-    for (int k = 0; k < NC - 2; ++k) A[r][k] = A[r][k + 1];
-    A[r][NC - 2] = t;
+// A lane's RPL rows of the NC columns in registers.  With an even RPL the rows
+// are packed in pairs (float2) so that a rotation updates two rows per
+// packed FP32x2 instruction; the results are those of the scalar FMAs.
+template <int RPL, int NC, bool PACK = (RPL % 2 == 0)>
+struct RegCols {
+  float2 v[RPL / 2][NC];
+  __device__ __forceinline__ float& operator()(int r, int k) {
+    return (r & 1) ? v[r >> 1][k].y : v[r >> 1][k].x;
   }
+  // columns i, j <- (c a_i - s a_j, s a_i + c a_j)
+  __device__ __forceinline__ void rotate(int i, int j, float cs, float sn) {
+    const float2 c2 = make_float2(cs, cs), s2 = make_float2(sn, sn), n2 = make_float2(-sn, -sn);
+#pragma unroll
+    for (int r = 0; r < RPL / 2; ++r) {
+      const float2 a = v[r][i], b = v[r][j];
+      v[r][i] = __ffma2_rn(c2, a, __fmul2_rn(n2, b));
+      v[r][j] = __ffma2_rn(s2, a, __fmul2_rn(c2, b));
+    }
+  }
+  // positions 0..NC-2 move down by one, position 0 to NC-2
+  __device__ __forceinline__ void shift() {
+#pragma unroll
+    for (int r = 0; r < RPL / 2; ++r) {
+      const float2 t = v[r][0];
+#pragma unroll
+      for (int k = 0; k < NC - 2; ++k) v[r][k] = v[r][k + 1];
+      v[r][NC - 2] = t;
+    }
+  }
+};
+template <int RPL, int NC>
+struct RegCols<RPL, NC, false> {
+  float v[RPL][NC];
+  __device__ __forceinline__ float& operator()(int r, int k) { return v[r][k]; }
+  __device__ __forceinline__ void rotate(int i, int j, float cs, float sn) {
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      const float a = v[r][i], b = v[r][j];
+      v[r][i] = fmaf(cs, a, -sn * b);
+      v[r][j] = fmaf(sn, a, cs * b);
+    }
+  }
+  __device__ __forceinline__ void shift() {
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      const float t = v[r][0];
+#pragma unroll
+      for (int k = 0; k < NC - 2; ++k) v[r][k] = v[r][k + 1];
+      v[r][NC - 2] = t;
+    }
+  }
+};
+
+template <int NC>
+__device__ __forceinline__ void shift_norms(float (&nrm)[NC]) {
   const float t = nrm[0];
 #pragma unroll
   for (int k = 0; k < NC - 2; ++k) nrm[k] = nrm[k + 1];
@@ -144,12 +190,13 @@ struct SvdSmem {
 };
 
 // residency target: the shared-memory form holds a round's column pairs in
-// registers, (NC/2) * 2 * RPL floats
+// registers, (NC/2) * 2 * RPL floats; the register form holds RPL * NC
+// floats twice over (sweeps, then the epilogue's fresh gather)
 template <int RPL, int NC, bool SM>
 constexpr int svd_minblocks() {
   return SM ? ((NC / 2) * 2 * RPL <= 64 ? PGSVT_SVD_MINBLOCKS_SM
                                         : ((NC / 2) * 2 * RPL <= 128 ? 2 : 1))
-            : PGSVT_SVD_MINBLOCKS;
+            : (RPL * NC >= 128 ? 2 : PGSVT_SVD_MINBLOCKS);
 }
 
 template <int RPL, int LANES, int NC, bool SM = false>
@@ -210,7 +257,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
   float* As = smem + (size_t)(wib * GROUPS + grp) * GSTRIDE;  // [NC][CS]
 
   // ---- gather B (svt.hpp:101-109)
-  float A[RPL][NC];
+  RegCols<RPL, NC> A;
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
     size_t base = 0;
@@ -223,7 +270,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
     for (int r = 0; r < RPL; ++r) {
       const float v = (colok && roff[r] >= 0) ? value(base + roff[r]) : 0.f;
       if constexpr (SM) As[k * CS + q * RPL + r] = v;
-      else A[r][k] = v;
+      else A(r, k) = v;
     }
   }
 
@@ -275,7 +322,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
       for (int k = 0; k < NC - 1; ++k) {
         float s = 0.f;
 #pragma unroll
-        for (int r = 0; r < RPL; ++r) s = fmaf(A[r][k], A[r][k], s);
+        for (int r = 0; r < RPL; ++r) s = fmaf(A(r, k), A(r, k), s);
         nrm[k] = lanes_sum<LANES>(s);
       }
       nrm[NC - 1] = 0.f;
@@ -287,7 +334,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
         for (int pp = 1; pp < NC / 2; ++pp) {
           float s = 0.f;
 #pragma unroll
-          for (int r = 0; r < RPL; ++r) s = fmaf(A[r][pp], A[r][NC - 1 - pp], s);
+          for (int r = 0; r < RPL; ++r) s = fmaf(A(r, pp), A(r, NC - 1 - pp), s);
           gm[pp] = s;
         }
 #pragma unroll
@@ -304,23 +351,19 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
           if (need) {
             float cs, sn;
             rotation(al, be, gv, g2, ab, cs, sn, definite, band);
-#pragma unroll
-            for (int r = 0; r < RPL; ++r) {
-              const float a = A[r][pi], b = A[r][pj];
-              A[r][pi] = fmaf(cs, a, -sn * b);
-              A[r][pj] = fmaf(sn, a, cs * b);
-            }
+            A.rotate(pi, pj, cs, sn);
             rotated_norms(al, be, gv, cs, sn, nrm[pi], nrm[pj]);
           }
         }
-        shift_round<RPL, NC>(A, nrm);
+        A.shift();
+        shift_norms<NC>(nrm);
       }
       if (__any_sync(0xffffffffu, definite)) continue;
       if (!__any_sync(0xffffffffu, band)) break;
 #pragma unroll
       for (int k = 0; k < NC; ++k)
 #pragma unroll
-        for (int r = 0; r < RPL; ++r) As[k * CS + q * RPL + r] = A[r][k];
+        for (int r = 0; r < RPL; ++r) As[k * CS + q * RPL + r] = A(r, k);
       __syncwarp();
       if (!fp64_again()) break;
     }
@@ -414,8 +457,8 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
         const float x = As[k * CS + q * RPL + r];
         s = fmaf(x, x, s);
       } else {
-        s = fmaf(A[r][k], A[r][k], s);
-        As[k * CS + q * RPL + r] = A[r][k];
+        s = fmaf(A(r, k), A(r, k), s);
+        As[k * CS + q * RPL + r] = A(r, k);
       }
     }
     sv[k] = sqrtf(lanes_sum<LANES>(s));

@@ -94,6 +94,36 @@ def test_alternative_svd_shape_matches_oracle(capi, pkg, oracle, bs, T):
     np.testing.assert_array_equal(Y2[:, :, f], Y0[:, :, f])
 
 
+@pytest.mark.parametrize("bs,T", [(4, 15), (4, 9), (8, 15), (7, 9)])
+def test_eight_rows_per_lane_shape_matches_oracle(capi, pkg, oracle, bs, T):
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=9, side=40, nt=T + 2)
+    X = noisy.astype(np.float64)
+    fr = (T // 2, T // 2 + 2)
+    base = dict(median_size=0, optimize_pgure=0, lambda_=0.5, block_size=bs, traj_length=T,
+                frame_begin=fr[0], frame_end=fr[1])
+    Y0, _, st0 = capi.denoise(X, capi.default_params(autotune=0, **base))
+    Y3, _, st3 = capi.denoise(X, capi.default_params(autotune=4, **base))
+    assert st0.svd_variant == 0 and st3.svd_variant == 3
+    Yo, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.5, block_size=bs,
+                              traj_length=T, frame_begin=fr[0], frame_end=fr[1], n_jobs=2)
+    f = slice(*fr)
+    scale = np.abs(Yo[:, :, f]).max()
+    assert np.abs(Y3[:, :, f] - Yo[:, :, f]).max() <= 1e-4 * scale
+    assert np.abs(Y3[:, :, f] - Y0[:, :, f]).max() <= 1e-4 * scale
+
+
+def test_eight_rows_per_lane_shape_with_pgure(capi, pkg, oracle):
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=8, side=48, nt=18)
+    base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, frame_begin=6, frame_end=10)
+    Y0, e0, _ = capi.denoise(noisy, capi.default_params(autotune=0, **base))
+    Y3, e3, st3 = capi.denoise(noisy, capi.default_params(autotune=4, **base))
+    assert st3.svd_variant == 3
+    f = slice(6, 10)
+    np.testing.assert_allclose(e3[f], e0[f], rtol=2e-3)
+    scale = np.abs(Y0[:, :, f]).max()
+    assert np.abs(Y3[:, :, f] - Y0[:, :, f]).max() <= 1e-3 * scale
+
+
 def test_shared_memory_svd_form_with_pgure(capi, pkg):
     noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=8, side=48, nt=18)
     base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, frame_begin=6, frame_end=10)
