@@ -419,22 +419,40 @@ def main():
         # median pre-filter 5, noise parameters estimated per window, PGURE on
         pd = capi.default_params(traj_length=15, block_size=args.patch, motion_window=7,
                                  median_size=5, random_seed=7, autotune=args.autotune)
-        step(pd)
-        torch.cuda.synchronize()
-        g0 = torch.cuda.Event(enable_timing=True)
-        g1 = torch.cuda.Event(enable_timing=True)
-        g0.record(stream)
-        std_ = step(pd)
-        g1.record(stream)
-        torch.cuda.synchronize()
-        dms = g0.elapsed_time(g1)
+
+        def timed_once(pp):
+            step(pp)
+            torch.cuda.synchronize()
+            g0 = torch.cuda.Event(enable_timing=True)
+            g1 = torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            step(pp)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            return g0.elapsed_time(g1)
+
+        dms = timed_once(pd)
+        dp_risk = risk.cpu().numpy().copy()
+        dp_evals = float(nev.cpu().numpy().mean())
+        dp_psnr = psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))
         line["default_path"] = {"value": nimg / (dms / 1e3), "unit": "frames/s",
-                                "ms_per_step": dms, "steps": 1,
-                                "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F")),
+                                "ms_per_step": dms, "steps": 1, "psnr_db": dp_psnr,
+                                "risk_evals_per_window": dp_evals,
                                 "noise_estimates_frame0": [float(v) for v in
                                                            est.cpu().numpy().reshape(4, nimg)[1:, 0]],
                                 "config": "median filter 5, alpha/mu/sigma estimated "
                                           "(noise method 4), PGURE on, same sequence"}
+        if not args.no_learned:  # the learned proposal on the default path
+            model = pkg.learned.load_model()
+            pd.lambda_model = model.ctypes.data
+            lms = timed_once(pd)
+            gap = (risk.cpu().numpy() - dp_risk) / np.abs(dp_risk)
+            line["default_path"]["learned"] = {
+                "value": nimg / (lms / 1e3), "unit": "frames/s", "ms_per_step": lms,
+                "risk_evals_per_window": float(nev.cpu().numpy().mean()),
+                "risk_gap_max": float(gap.max()), "risk_gap_mean": float(gap.mean()),
+                "windows_gap_le_1pct": float(np.mean(gap <= 0.01)),
+                "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
     if args.batch:
         line["batch"] = run_batch(capi, args.batch, args.seed)
     if not args.no_cpu_baseline:

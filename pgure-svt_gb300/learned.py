@@ -20,18 +20,21 @@ from . import _capi, synth
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODEL_PATH = os.path.join(HERE, "lambda_mlp.npz")
 SIDES = (128, 192, 256, 320, 384, 448, 512)
+POW2_SIDES = (128, 256, 512)
 UPPER = 100.0
 SEQ_FRAMES = 18          # frames 7..10 are full windows of a T=15 trajectory
 LABEL_FRAMES = (7, 11)
 
 
-def random_sequence(seed):
+def random_sequence(seed, estimated=False):
     """A seeded sequence of the training distribution: 128^2-512^2, blob or
     blob+lattice scenes, integer or sub-pixel drift, alpha in [0.05, 1],
     mu in [0, 2], sigma in [0.5, 5] (raw counts).  Returns (noisy float32,
-    (alpha, mu, sigma))."""
+    (alpha, mu, sigma)), or (noisy, None) with `estimated`: a power-of-two
+    side (the noise estimator's F-test table has no other sizes) for the
+    reference's default path, which estimates the noise parameters."""
     rng = np.random.default_rng(seed)
-    side = int(rng.choice(SIDES))
+    side = int(rng.choice(POW2_SIDES if estimated else SIDES))
     nblobs = max(1, int(round(300 * (side / 512.0) ** 2 * rng.uniform(0.3, 1.5))))
     lattice = bool(rng.random() < 0.5)
     integer = bool(rng.random() < 0.3)
@@ -42,14 +45,17 @@ def random_sequence(seed):
     clean = synth.blobs(side, SEQ_FRAMES, nblobs, int(rng.integers(1 << 31)), max_step, integer,
                         lattice)
     noisy = synth.poisson_gaussian(clean, alpha, mu, sigma, int(rng.integers(1 << 31)))
-    return np.asfortranarray(noisy.astype(np.float32)), (alpha, mu, sigma)
+    return np.asfortranarray(noisy.astype(np.float32)), (None if estimated else (alpha, mu, sigma))
 
 
 def search_params(noise, frames=None, model=None, **kw):
     """Parameters of the benchmark's PGURE search (4x4 patches, T=15,
-    motion window 7, reference compat mode, probe seed 7)."""
-    a, m, s = noise
-    p = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7, median_size=0,
+    motion window 7, reference compat mode, probe seed 7) with the given
+    noise parameters, or with noise=None the reference's defaults: median
+    pre-filter 5 and the noise parameters estimated per window."""
+    a, m, s = noise if noise is not None else (-1.0, -1.0, -1.0)
+    p = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7,
+             median_size=0 if noise is not None else 5,
              optimize_pgure=1, motion_estimation=1, alpha=a, mu=m, sigma=s, random_seed=7)
     if frames is not None:
         p.update(frame_begin=frames[0], frame_end=frames[1])
@@ -68,7 +74,8 @@ def target(lam):
 
 
 def label(noisy, noise, frames=LABEL_FRAMES):
-    """Features and plain-search labels of frames [frames[0], frames[1])."""
+    """Features and plain-search labels of frames [frames[0], frames[1])
+    (noise=None: the reference's default path, noise estimated)."""
     p = search_params(noise, frames)
     _, est, st, ex = _capi.denoise_ex(noisy, p, features=True)
     f0, f1 = frames
@@ -77,14 +84,20 @@ def label(noisy, noise, frames=LABEL_FRAMES):
                 lambdas=lam, risks=ex["risk"][f0:f1].copy(), evals=ex["evals"][f0:f1].copy())
 
 
-def training_set(n_seq, seed=0, pool=None):
-    """Labelled windows of n_seq random sequences (4 windows each).  `pool`
-    (a process pool started before any GPU call) generates sequences in the
-    background while the GPU labels."""
+def training_set(n_seq, seed=0, pool=None, estimated=False):
+    """Labelled windows of n_seq random sequences (4 windows each), with
+    given or (estimated=True) estimated noise parameters.  `pool` (a process
+    pool started before any GPU call) generates sequences in the background
+    while the GPU labels."""
     seeds = [seed * 1000003 + i for i in range(n_seq)]
-    gen = pool.imap(random_sequence, seeds, chunksize=2) if pool else map(random_sequence, seeds)
+    fn = _gen_estimated if estimated else random_sequence
+    gen = pool.imap(fn, seeds, chunksize=2) if pool else map(fn, seeds)
     parts = [label(noisy, noise) for noisy, noise in gen]
     return {k: np.concatenate([q[k] for q in parts]) for k in parts[0]}
+
+
+def _gen_estimated(seed):
+    return random_sequence(seed, estimated=True)
 
 
 def init_model(features, targets, seed=0):

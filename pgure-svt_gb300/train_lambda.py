@@ -1,11 +1,14 @@
 """Train the learned lambda proposal and write the shipped model.
 
-    python pgure-svt_gb300/train_lambda.py --sequences 2000 --held-out 20 \\
-        --out pgure-svt_gb300/lambda_mlp.npz --report lambda_report.json
+    python pgure-svt_gb300/train_lambda.py --sequences 2000 --estimated 1000 \\
+        --held-out 20 --out pgure-svt_gb300/lambda_mlp.npz --report lambda_report.json
 
 Steps (all compute on the GPU through libpgsvt.so):
 1. label: for each seeded random sequence (learned.random_sequence), the plain
-   PGURE search of windows 7..10 gives (features, log10(lambda*/100));
+   PGURE search of windows 7..10 gives (features, log10(lambda*/100)); the
+   `--sequences` ones with their noise parameters given, the `--estimated`
+   ones on the reference's default path (median pre-filter 5, noise
+   parameters estimated per window);
 2. train: pgsvt_lambda_train (bf16 weights, FP32 accumulation, AdamW,
    one CUDA graph per epoch) from learned.init_model;
 3. evaluate on held-out sequences: prediction error, and plain vs learned
@@ -41,11 +44,15 @@ def _gen(seed):  # pool worker: the package is imported per process
     return _package().learned.random_sequence(seed)
 
 
-def evaluate(pkg, model, seeds, pool):
+def _gen_est(seed):
+    return _package().learned.random_sequence(seed, estimated=True)
+
+
+def evaluate(pkg, model, seeds, pool, estimated=False):
     """Held-out windows: prediction error, plain vs learned search."""
     L = pkg.learned
     rows = []
-    for noisy, noise in pool.imap(_gen, seeds):
+    for noisy, noise in pool.imap(_gen_est if estimated else _gen, seeds):
         lab = L.label(noisy, noise)
         res = L.compare(noisy, noise, model, frames=L.LABEL_FRAMES)
         f0, f1 = L.LABEL_FRAMES
@@ -71,6 +78,8 @@ def evaluate(pkg, model, seeds, pool):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--sequences", type=int, default=2000)
+    ap.add_argument("--estimated", type=int, default=1000,
+                    help="sequences labelled on the default path (noise estimated)")
     ap.add_argument("--held-out", type=int, default=20)
     ap.add_argument("--epochs", type=int, default=600)
     ap.add_argument("--batch", type=int, default=256)
@@ -87,9 +96,17 @@ def main():
     pool = mp.get_context("spawn").Pool(a.workers)  # before any GPU call
     pkg = _package()
     L = pkg.learned
+    held = [10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out)]
+    held_est = [2 * 10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out)]
+
+    def evaluate_both(model):
+        ev = evaluate(pkg, model, held, pool) if a.held_out else {}
+        if a.held_out and a.estimated:
+            ev["estimated"] = evaluate(pkg, model, held_est, pool, estimated=True)
+        return ev
+
     if a.evaluate:
-        held = [10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out)]
-        ev = evaluate(pkg, L.load_model(a.evaluate), held, pool)
+        ev = evaluate_both(L.load_model(a.evaluate))
         pool.close()
         pool.join()
         print(json.dumps(ev))
@@ -100,6 +117,9 @@ def main():
     t0 = time.time()
     seeds = [a.seed * 1000003 + i for i in range(a.sequences)]
     parts = [L.label(noisy, noise) for noisy, noise in pool.imap(_gen, seeds, chunksize=2)]
+    n_given = sum(len(q["targets"]) for q in parts)
+    seeds = [5 * 10 ** 6 + a.seed * 1000003 + i for i in range(a.estimated)]
+    parts += [L.label(noisy, noise) for noisy, noise in pool.imap(_gen_est, seeds, chunksize=2)]
     data = {k: np.concatenate([q[k] for q in parts]) for k in parts[0]}
     t_label = time.time() - t0
     if a.data:
@@ -108,13 +128,16 @@ def main():
     model, curve = L.train(data["features"], data["targets"], epochs=a.epochs, batch=a.batch,
                            seed=a.seed, lr=a.lr)
     t_train = time.time() - t1
-    held = [10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out)]
-    ev = evaluate(pkg, model, held, pool) if a.held_out else {}
+    ev = evaluate_both(model)
     pool.close()
     pool.join()
-    L.save_model(model, a.out, n_train=len(data["targets"]), epochs=a.epochs,
+    L.save_model(model, a.out, n_train=len(data["targets"]), n_estimated=len(data["targets"]) - n_given,
+                 epochs=a.epochs,
                  final_loss=float(curve[-1]), seed=a.seed)
-    rep = dict(train_windows=int(len(data["targets"])), label_seconds=t_label,
+    est = slice(n_given, None)
+    rep = dict(train_windows=int(len(data["targets"])), estimated_windows=int(len(data["targets"]) - n_given),
+               plain_evals_estimated=float(data["evals"][est].mean()) if a.estimated else None,
+               label_seconds=t_label,
                train_seconds=t_train, epochs=a.epochs, loss_first=float(curve[0]),
                loss_last=float(curve[-1]), target_mean=float(data["targets"].mean()),
                target_std=float(data["targets"].std()),
