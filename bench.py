@@ -51,6 +51,9 @@ def parse():
                     help="skip timing the reference's default path (median 5 + noise estimation)")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time pgsvt_denoise_batch on this many uneven sequences")
+    ap.add_argument("--batch-full", action="store_true",
+                    help="batch sequences of the full configuration (sides to 1024, 30-300 "
+                         "frames) instead of the bench-time scaled ones")
     ap.add_argument("--autotune", type=int, default=1,
                     help="SVD kernel form: 1 tuned (default), 0 registers, 2 more lanes, "
                     "3 shared memory, 4 eight rows per lane")
@@ -133,31 +136,47 @@ def svd_flops(m, n):
     return 14 * m * n * n + 8 * n ** 3
 
 
-def batch_workload(n, seed):
-    """Sequences of the uneven-batch configuration, scaled to bench time:
-    sides {128, 256, 384, 512}, 30-45 frames, patch {4, 6, 8}, trajectory
-    {9, 15, 21}, alpha U[0.05, 1], sigma U[0.5, 5], the blob generator with
-    sub-pixel drift; 16 fixed lambda values per sequence."""
+def _batch_sequence(spec):
+    """One sequence of the uneven-batch workload (a spawn-pool worker)."""
+    i, seed, full = spec
     pkg = entry.load_package()
-    rng = np.random.default_rng(seed)
-    out = []
-    for i in range(n):
-        side = int(rng.choice([128, 256, 384, 512]))
-        nt = int(rng.integers(30, 46))
-        bs = int(rng.choice([4, 6, 8]))
-        T = int(rng.choice([9, 15, 21]))
-        a, sg = float(rng.uniform(0.05, 1.0)), float(rng.uniform(0.5, 5.0))
-        nb = max(1, int(round(80 * (side / 256.0) ** 2)))
-        clean = pkg.synth.blobs(side, nt, nb, seed * 1000 + i, 2.0, False, False)
-        noisy = pkg.synth.poisson_gaussian(clean, a, 0.5, sg, seed * 1000 + i + 1)
-        lam = np.geomspace(1e-3, 100.0, 16) * float(rng.uniform(0.5, 2.0))
-        out.append(dict(X=np.asfortranarray(noisy.astype(np.float32)), bs=bs, T=T,
-                        noise=(a, 0.5, sg), lambdas=lam))
-    return out
+    rng = np.random.default_rng([seed, i])
+    side = int(rng.choice([128, 256, 384, 512, 1024] if full else [128, 256, 384, 512]))
+    nt = int(rng.integers(30, 301)) if full else int(rng.integers(30, 46))
+    bs = int(rng.choice([4, 6, 8]))
+    T = int(rng.choice([9, 15, 21]))
+    a, sg = float(rng.uniform(0.05, 1.0)), float(rng.uniform(0.5, 5.0))
+    nb = max(1, int(round(80 * (side / 256.0) ** 2)))
+    clean = pkg.synth.blobs(side, nt, nb, seed * 1000 + i, 2.0, False, False)
+    noisy = pkg.synth.poisson_gaussian(clean, a, 0.5, sg, seed * 1000 + i + 1)
+    lam = np.geomspace(1e-3, 100.0, 16) * float(rng.uniform(0.5, 2.0))
+    return dict(X=np.asfortranarray(noisy.astype(np.float32)), bs=bs, T=T,
+                noise=(a, 0.5, sg), lambdas=lam)
 
 
-def run_batch(capi, n, seed, slots=2):
-    seqs = batch_workload(n, seed)
+def batch_workload(n, seed, full=False):
+    """Sequences of the uneven-batch configuration: sides {128, 256, 384,
+    512, 1024}, 30-300 frames (full=True), or scaled to bench time: sides up
+    to 512, 30-45 frames; patch {4, 6, 8}, trajectory {9, 15, 21}, alpha
+    U[0.05, 1], sigma U[0.5, 5], the blob generator with sub-pixel drift; 16
+    fixed lambda values per sequence.  Generated in a spawn process pool."""
+    import multiprocessing as mp
+    specs = [(i, seed, full) for i in range(n)]
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    os.environ.update(OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")  # one core per worker
+    try:
+        with mp.get_context("spawn").Pool(max(1, min(16, (os.cpu_count() or 2) - 1))) as pool:
+            return pool.map(_batch_sequence, specs, chunksize=1)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def run_batch(capi, n, seed, slots=2, full=False):
+    seqs = batch_workload(n, seed, full)
     inp = []
     for q in seqs:
         a, m, s = q["noise"]
@@ -180,9 +199,12 @@ def run_batch(capi, n, seed, slots=2):
             "value": frames / dt, "unit": "frames/s (e2e, host buffers)", "slots": slots,
             "risk_evals_per_window": st.risk_evals / max(1, st.windows),
             "gpu_launches": int(st.kernel_launches),
-            "config": "sides {128,256,384,512}, 30-45 frames, patch {4,6,8}, T {9,15,21}, "
-                      "16 fixed lambda per sequence (uneven-batch configuration scaled to "
-                      "%d sequences)" % n}
+            "config": ("sides {128,256,384,512,1024}, 30-300 frames, patch {4,6,8}, T {9,15,21}, "
+                       "16 fixed lambda per sequence (uneven-batch configuration, %d sequences)" % n)
+                      if full else
+                      ("sides {128,256,384,512}, 30-45 frames, patch {4,6,8}, T {9,15,21}, "
+                       "16 fixed lambda per sequence (uneven-batch configuration scaled to "
+                       "%d sequences)" % n)}
 
 
 def cpu_baseline(noisy, nm, bs, evals_per_window, stride, threads, nsample):
@@ -454,7 +476,7 @@ def main():
                 "windows_gap_le_1pct": float(np.mean(gap <= 0.01)),
                 "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
     if args.batch:
-        line["batch"] = run_batch(capi, args.batch, args.seed)
+        line["batch"] = run_batch(capi, args.batch, args.seed, full=args.batch_full)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(noisy, (a, m, s), args.patch, evals_per_window,

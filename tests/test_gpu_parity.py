@@ -239,6 +239,28 @@ def test_frame_range_shards_sum_to_full_run(capi, pkg, g):
     np.testing.assert_array_equal(sum(parts), Y)
 
 
+def test_largest_frames_identity_and_shards(capi, pkg):
+    """1024 x 1024 frames (the largest side of the uneven-batch
+    configuration), where position and voxel indices reach their widest
+    ranges.  A fixed lambda large enough that the exponential weights
+    shrink nothing (svt.hpp:137: the threshold smax exp(-lambda s^2 / 2)
+    underflows) rebuilds every patch, so the output is the input; and two
+    frame ranges give the frames of one full run, bit for bit."""
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=31, side=1024, nt=16)
+    X = noisy.astype(np.float32)
+    kw = dict(median_size=-1, optimize_pgure=0, lambda_=1e12)
+    Y, _, st = capi.denoise(X, capi.default_params(**kw))
+    assert st.windows == 16
+    err = np.abs(Y - X).max() / np.abs(X).max()
+    print("max relative difference to the input", err)
+    assert err < 1e-5
+    kw["lambda_"] = 0.1
+    Y, _, _ = capi.denoise(X, capi.default_params(**kw))
+    parts = [capi.denoise(X, capi.default_params(frame_begin=b, frame_end=e, **kw))[0]
+             for b, e in ((0, 7), (7, 16))]
+    np.testing.assert_array_equal(parts[0] + parts[1], Y)
+
+
 # ---- median pre-filter of the ARPS input
 
 def test_median_filter_matches_reference_fixtures(capi):
