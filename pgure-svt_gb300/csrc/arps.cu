@@ -75,8 +75,8 @@ struct Block {
       for (int r = 0; r < nb; ++r) {
         const int a = (int)at(r + cc * nb, nb);
         const int b = (int)__ldg(c.xa2 + (y + r) + (size_t)(x + cc) * c.S);
-        const long long d = a - b;
-        acc += (unsigned long long)(d * d);
+        const unsigned d = (unsigned)abs(a - b);  // < 2^19
+        acc += (unsigned long long)d * d;
       }
     return acc;
   }
@@ -142,48 +142,59 @@ __device__ __forceinline__ double src64(const ArpsCtx& c, const float* xf, const
 // Per-warp scratch of the exact (FP64) decisions.
 template <int BS>
 struct ArpsWarp {
-  static constexpr int kSq = BS > 0 ? 128 : 256;  // squared differences per pass
+  static constexpr int kSq = 256;  // squared differences per pass
   double sq[kSq];
-  double cst[6];      // exact cost per slot
-  uint32_t pos[6];    // candidate (y, x) per slot, 16 bits each
-  int bi, bj;         // reference block
-  unsigned em;        // slots to evaluate
+  double cst[32 * 6];     // exact cost per (lane, slot)
+  uint32_t pos[32 * 6];   // candidate (y, x) per (lane, slot), 16 bits each
+  uint32_t blk[32];       // reference block (i, j) per lane, 16 bits each
+  uint16_t cand[32 * 6];  // the warp's candidates to evaluate: lane * 6 + slot
 };
-
-__device__ __forceinline__ int nth_slot(unsigned em, int n) {
-  for (int k = 0; k < 6; ++k)
-    if ((em >> k) & 1u) {
-      if (n == 0) return k;
-      --n;
-    }
-  return 0;
-}
 
 // Exact reference costs (arps.hpp:148-151 as the reference evaluates them:
 // FP64 x/umax, FP64 squares, Armadillo's two-accumulator accu(), no fused
-// multiply-add) of the slots ws.em for the block at (ws.bi, ws.bj), by the
-// whole warp: the squared differences are spread over the lanes, and the
-// even- and odd-element accumulators of every slot are summed in element
-// order by two lanes.  The FP64 pipe runs a warp instruction at a fraction of
-// the FP32 rate whatever its active lanes, so one lane's exact step costs about
-// a tenth of the FP64 instructions of a per-thread evaluation.
+// multiply-add) of every slot in `em` of every lane, computed by the whole
+// warp at once: the squared differences of all candidate blocks are spread
+// over the lanes, and the even- and odd-element accumulators of every
+// candidate are summed in element order by two lanes.  The FP64 pipe runs a
+// warp instruction at a fraction of the FP32 rate whatever its active lanes,
+// so this takes a small part of the FP64 instructions (and of the latency) of
+// per-thread evaluations.  Results in ws.cst[lane * 6 + slot].
 template <int BS>
-__device__ void warp_cost64(const ArpsCtx& c, ArpsWarp<BS>& ws) {
+__device__ void warp_cost64(const ArpsCtx& c, ArpsWarp<BS>& ws, unsigned em, int i, int j,
+                            int y, int x, const int (*off)[2], int nslot) {
   const int lane = threadIdx.x & 31;
   const int nb = BS > 0 ? BS : c.bs;
   const int m = nb * nb;
   const double oo = 1.0 / (double)m;
-  const unsigned em = ws.em;
-  const int nc = __popc(em);
-  const int per = m >= ArpsWarp<BS>::kSq ? 1 : ArpsWarp<BS>::kSq / m;
-  for (int c0 = 0; c0 < nc; c0 += per) {
-    const int cn = min(per, nc - c0);
+  // this lane's candidates, and their place in the warp's list
+  const int mine = __popc(em);
+  int first = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, first, o);
+    if (lane >= o) first += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, first, 31);
+  first -= mine;
+  if (em) {
+    ws.blk[lane] = ((uint32_t)i & 0xffffu) | ((uint32_t)j << 16);
+    int r = first;
+    for (int k = 0; k < nslot; ++k) {
+      if (!((em >> k) & 1u)) continue;
+      ws.pos[lane * 6 + k] = ((uint32_t)(y + off[k][1]) & 0xffffu) | ((uint32_t)(x + off[k][0]) << 16);
+      ws.cand[r++] = (uint16_t)(lane * 6 + k);
+    }
+  }
+  __syncwarp();
+  const int per = min(16, ArpsWarp<BS>::kSq / m);  // two summing lanes per candidate
+  for (int c0 = 0; c0 < total; c0 += per) {
+    const int cn = min(per, total - c0);
     for (int t = lane; t < cn * m; t += 32) {
-      const int k = nth_slot(em, c0 + t / m);
+      const int cd = ws.cand[c0 + t / m];
       const int e = t % m, r = e % nb, cc = e / nb;
-      const uint32_t pk = ws.pos[k];
+      const uint32_t pb = ws.blk[cd / 6], pk = ws.pos[cd];
+      const int bi = (int)(pb & 0xffffu), bj = (int)(pb >> 16);
       const int py = (int)(pk & 0xffffu), px = (int)(pk >> 16);
-      const size_t ka = (ws.bi + r) + (size_t)(ws.bj + cc) * c.S;
+      const size_t ka = (bi + r) + (size_t)(bj + cc) * c.S;
       const size_t kb = (py + r) + (size_t)(px + cc) * c.S;
       const double a = c.pa1 ? c.pa1[ka] : __ddiv_rn(src64(c, c.xa1, c.xa1d, ka), c.umax);
       const double b = c.pa2 ? c.pa2[kb] : __ddiv_rn(src64(c, c.xa2, c.xa2d, kb), c.umax);
@@ -198,7 +209,7 @@ __device__ void warp_cost64(const ArpsCtx& c, ArpsWarp<BS>& ws) {
     }
     const double v2 = __shfl_down_sync(0xffffffffu, v, 1);
     if (lane < 2 * cn && !(lane & 1))
-      ws.cst[nth_slot(em, c0 + (lane >> 1))] = __dmul_rn(__dadd_rn(v, v2), oo);
+      ws.cst[ws.cand[c0 + (lane >> 1)]] = __dmul_rn(__dadd_rn(v, v2), oo);
     __syncwarp();
   }
 }
@@ -380,19 +391,10 @@ __device__ void arps_pair(const ArpsCtx& c, bool live, int it, int& my, int& mx,
     if (!done)
       ks = c.integer ? decide_int<BS>(c, blk, cd, ev, off, nslot, y, x, em)
                      : decide_f32(cs, es, ev, nslot, em);
-    for (unsigned want = __ballot_sync(0xffffffffu, em != 0u); want; want &= want - 1u) {
-      const int L = __ffs(want) - 1;
-      if (lane == L) {
-        for (int k = 0; k < nslot; ++k)
-          ws.pos[k] = ((uint32_t)(y + off[k][1]) & 0xffffu) | ((uint32_t)(x + off[k][0]) << 16);
-        ws.bi = i;
-        ws.bj = j;
-        ws.em = em;
-      }
-      __syncwarp();
-      warp_cost64<BS>(c, ws);
-      if (lane == L) {
-        ks = resolve_exact(c.integer, ws.cst, em, nslot);
+    if (__any_sync(0xffffffffu, em != 0u)) {
+      warp_cost64<BS>(c, ws, em, i, j, y, x, off, nslot);
+      if (em) {
+        ks = resolve_exact(c.integer, ws.cst + lane * 6, em, nslot);
         ++nexact;
       }
       __syncwarp();
