@@ -414,6 +414,28 @@ def main():
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         roof["traffic"] = json.load(open(prof)).get("k_svd")
+    # In the timed region the SVD of one window batch shares the GPU with the
+    # other streams' lambda searches, so its event time overstates the
+    # kernels' own.  The same launches alone: one batch of windows (the
+    # library's batch size for this frame), hence one stream, after the
+    # timed region.
+    npatch = (S - args.patch + 1) ** 2
+    wb = max(1, min(nimg, (500000 + npatch - 1) // npatch))
+    pi = params(capi, a, m, s, args.patch, args.hint, args.autotune)
+    pi.frame_begin, pi.frame_end = nimg // 2 - wb // 2, nimg // 2 - wb // 2 + wb
+    iso = []
+    for _ in range(4):
+        sti = step(pi)
+        iso.append(sti.stage_seconds[4] / max(1, sti.svd_launches))
+    torch.cuda.synchronize()
+    iso_t = min(iso[1:])
+    iso_flop = svd_flops(M, N) * sti.svd_matrices / max(1, sti.svd_launches)
+    roof.update({"isolated_launch_ms": iso_t * 1e3,
+                 "achieved_isolated": iso_flop / iso_t / 1e12,
+                 "frac_isolated": iso_flop / iso_t / 1e12 / fp32_peak,
+                 "isolated_note": "the same SVD launch (%d windows x %d copies) with no other "
+                                  "stream running, after the timed region" % (wb, sti.svd_matrices
+                                  // max(1, sti.svd_launches) // npatch // wb or 1)})
 
     evals_per_window = max(1, round(st.risk_evals / max(1, st.windows)))
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
@@ -435,7 +457,8 @@ def main():
             "svd_fp64_tests": int(st.svd_fp64_tests),
             "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8),
             "svd_variant": {0: "registers", 1: "more lanes per patch",
-                            2: "shared memory"}.get(int(st.svd_variant), "?")}
+                            2: "shared memory", 3: "eight rows per lane",
+                            4: "QR-preconditioned"}.get(int(st.svd_variant), "?")}
     if not args.no_default_path:
         # the reference's default configuration (SVT() / PGURE-SVT defaults):
         # median pre-filter 5, noise parameters estimated per window, PGURE on

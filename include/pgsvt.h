@@ -114,11 +114,15 @@ typedef struct {
                                window batch of each patch size / window
                                length seen by the process and keep the
                                fastest (results agree to FP32 rounding);
-                               0: the default shape; 2: more lanes per
-                               patch where the patch size has that form;
-                               3: the default shape with its columns in
-                               shared memory; 4: 8 rows per lane (patch
-                               sides <= 4 and 7..8, windows <= 16)           */
+                               0: the default shape (the QR-preconditioned
+                               form for 7x7 and 8x8 patches and windows
+                               <= 15 frames, else the register form);
+                               2: more lanes per patch where the patch size
+                               has that form; 3: the register form with
+                               its columns in shared memory; 4: 8 rows per
+                               lane (patch sides <= 4 and 7..8, windows
+                               <= 15); 5: the QR-preconditioned form (patch
+                               sides 5..8, windows <= 15)                    */
 } pgsvt_params;
 
 /* Optional per-frame outputs of pgsvt_denoise_ex / pgsvt_denoise_device_ex

@@ -354,7 +354,7 @@ Problem make_problem(const pgsvt_params& p, const Setup& su) {
   pb.hint_rounds = p.hint_rounds ? (int)p.hint_rounds : 1;
   pb.hint_flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
   pb.acc64 = 0;
-  pb.svd_variant = 0;
+  pb.svd_variant = svd_default_variant(pb.g.M, pb.g.NC);
   pb.fixed = nullptr;
   pb.nfixed = 0;
   pb.fixed_risk = nullptr;
@@ -374,6 +374,7 @@ size_t window_bytes(const Problem& pb) {
   b += NC * g.M * NP * 4;           // U0
   b += NC * g.nwin * NP * 4;        // V0
   b += 2 * 4 * NC * NP * 4 + NP * 4;  // sv, hv, nlive0
+  if (svd_split_scratch(g.M, g.NC)) b += 4 * NP * NC * (16 + 1) * 4;  // xq, xqn
   b += (size_t)pb.K * C * (pb.acc64 ? 8 : 4);  // acc
   b += (size_t)pb.K * ((NP + 31) / 32 + mse_blocks(g)) * 8 + 256 * 8;  // partials
   b += sizeof(WinConst) + sizeof(SearchState) + 2 * (size_t)g.fw * sizeof(ArpsChain);
@@ -452,7 +453,7 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   bool tune = false;
   if (p.autotune >= 2) {  // forced: shape autotune - 1 where the patch size has it
     const int v = (int)p.autotune - 1;
-    pb.svd_variant = svd_variant_ok(pb.g.M, pb.g.NC, v) ? v : 0;
+    pb.svd_variant = svd_variant_ok(pb.g.M, pb.g.NC, v) ? v : svd_default_variant(pb.g.M, pb.g.NC);
   } else if (p.autotune) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(tkey);
@@ -729,6 +730,11 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     d.sv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
     d.hv = mem.arr<float>((size_t)W * 4 * g.NC * g.NP);
     d.nlive0 = mem.arr<int32_t>((size_t)W * g.NP);
+    if (svd_split_scratch(g.M, g.NC)) {
+      const size_t items = (size_t)W * ncopies * g.NP;
+      d.xq = mem.arr<float>(items * g.NC * 16);
+      d.xqn = mem.arr<float>(items * g.NC);
+    }
     PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * (size_t)W * 4 * g.NC * g.NP, L.s));
     const size_t accb = (size_t)W * pb.K * C * (pb.acc64 ? 8 : 4);
     d.acc = mem.get(accb);
@@ -1065,6 +1071,10 @@ struct OneWindow {
     d.sv = mem.arr<float>((size_t)4 * g.NC * g.NP);
     d.hv = mem.arr<float>((size_t)4 * g.NC * g.NP);
     d.nlive0 = mem.arr<int32_t>(g.NP);
+    if (svd_split_scratch(g.M, g.NC)) {
+      d.xq = mem.arr<float>((size_t)ncopies * g.NP * g.NC * 16);
+      d.xqn = mem.arr<float>((size_t)ncopies * g.NP * g.NC);
+    }
     PGSVT_CK(cudaMemsetAsync(d.hv, 0, sizeof(float) * 4 * g.NC * g.NP, s));
     pb.acc64 = 1;  // a caller-given trajectory table may stack any number of patches
     d.acc = mem.get(sizeof(unsigned long long) * pb.K * g.cube());

@@ -157,6 +157,8 @@ struct DeviceBuffers {
   float* V0;
   float* sv;
   float* hv;
+  float* xq;               // split SVD forms' scratch: [items][NC][X rows] (svd_qr.cu)
+  float* xqn;              // its column norms [items][NC]
   int32_t* nlive0;         // [W][NP] singular triplets of copy 0 that can survive
   void* acc;               // [W][K][nwin][S*S] int32 or int64 fixed point
   double* part_lin;        // [W][K][nblk_eval]
@@ -285,8 +287,11 @@ void set_last_error(const std::string& m);
 int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
 int svd_columns(int nwin);
-constexpr int kSvdVariants = 4;
+constexpr int kSvdVariants = 5;
 int svd_variants(int M, int NC);
+bool svd_qr_form(int M, int NC);  // the QR-preconditioned SVD applies (its scratch is needed)
+int svd_default_variant(int M, int NC);
+bool svd_split_scratch(int M, int NC);  // a split SVD form applies (xq, xqn needed)
 bool svd_variant_ok(int M, int NC, int v);
 bool svd_supported(int bs, int nwin);
 

@@ -27,6 +27,10 @@ namespace pgsvt {
 namespace svdk {
 template <int RPL, int LANES, int NC, bool SM>
 cudaError_t run_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+template <int NC>
+cudaError_t run_svd_qr(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+template <int NC>
+cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 }
 
 int svd_columns(int nwin) {
@@ -49,16 +53,28 @@ bool svd_supported(int bs, int nwin) {
 // default shape with the columns in shared memory (addressed by the round's
 // schedule, no moves), variant 3 holds 8 rows per lane in fewer lanes (the
 // per-pair rotation arithmetic, replicated in every lane of a patch, is shared
-// by twice the rows; 2 resident blocks per SM instead of 3).  Variants 0 and 2
-// apply the same rotations in the same order; all agree to FP32 rounding.  The
-// autotuner (capi.cu) times them on the caller's data and keeps the fastest.
+// by twice the rows; 2 resident blocks per SM instead of 3), variant 4
+// (patches of 17..64 rows, windows <= 15) sweeps the triangle of B's QR
+// factorisation instead of B (svd_qr.cu).  For patches of at most 16 rows
+// and windows of at most 15 frames variant 0 runs its sweeps and its factors
+// in two kernels (svd_qr.cu; the sweeps without the factors' registers fit
+// four resident blocks per SM instead of three), with identical results,
+// wherever the caller provides the scratch (not in the allocation-free entry).  Variants 0 and 2 apply the same
+// rotations in the same order; all agree to FP32 rounding.  The autotuner
+// (capi.cu) times them on the caller's data and keeps the fastest.
 bool svd_variant_ok(int M, int NC, int v) {
   if (M > 64) return v == 0;  // patch sides 9..16: the shared-memory form only
   if (v == 0 || v == 2) return true;
   if (v == 1) return !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
   if (v == 3) return NC <= 16 && (M <= 16 || M > 40);  // 8 x 2 and 8 x 8 lanes
+  if (v == 4) return svd_qr_form(M, NC);                 // QR-preconditioned
   return false;
 }
+bool svd_qr_form(int M, int NC) { return M > 16 && M <= 64 && NC <= 16; }
+bool svd_split_scratch(int M, int NC) { return svd_qr_form(M, NC) || (M <= 16 && NC <= 16); }
+// the untuned shape: the QR-preconditioned form for 7x7 and 8x8 patches
+// (2.2x faster than their 64-row register form on 512^2 windows), else 0
+int svd_default_variant(int M, int NC) { return (M > 40 && svd_qr_form(M, NC)) ? 4 : 0; }
 int svd_variants(int M, int NC) {
   int n = 0;
   for (int v = 0; v < kSvdVariants; ++v) n += svd_variant_ok(M, NC, v);
@@ -75,6 +91,14 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
   using namespace svdk;
   const int M = pb.g.M, NC = pb.g.NC;
   const bool alt = pb.svd_variant == 1;
+  if (pb.svd_variant == 4 && M > 16 && M <= 64) {  // QR-preconditioned
+    if (NC == 10) return run_svd_qr<10>(pb, d, s);
+    if (NC == 16) return run_svd_qr<16>(pb, d, s);
+  }
+  if (pb.svd_variant == 0 && M <= 16 && d.xq && d.xqn) {  // sweeps and factors in two kernels
+    if (NC == 10) return run_svd_split<10>(pb, d, s);
+    if (NC == 16) return run_svd_split<16>(pb, d, s);
+  }
   if (pb.svd_variant == 3 && NC <= 16) {  // 8 rows per lane
     if (M <= 16) {
       if (NC == 10) return run_svd<8, 2, 10, false>(pb, d, s);

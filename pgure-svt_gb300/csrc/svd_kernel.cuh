@@ -199,6 +199,108 @@ constexpr int svd_minblocks() {
             : (RPL * NC >= 128 ? 2 : PGSVT_SVD_MINBLOCKS);
 }
 
+// Only near-degenerate pairs moved, by amounts at the FP32 noise level of
+// their inner products: decide convergence from FP64 inner products of the
+// current columns (exact products of the FP32 entries) staged in As
+// ([NC][CS], this lane's RPL rows at q * RPL).
+template <int RPL, int LANES, int CS>
+__device__ bool fp64_check(const float* As, int q, int nwin, unsigned& fp64_tests) {
+  bool again = false;
+  for (int i = 0; i < nwin; ++i) {
+    for (int j = i + 1; j < nwin; ++j) {
+      float gi = 0.f, ai = 0.f, aj = 0.f;
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) {
+        const float x = As[i * CS + q * RPL + r], y = As[j * CS + q * RPL + r];
+        gi = fmaf(x, y, gi);
+        ai = fmaf(x, x, ai);
+        aj = fmaf(y, y, aj);
+      }
+      gi = lanes_sum<LANES>(gi);
+      ai = lanes_sum<LANES>(ai);
+      aj = lanes_sum<LANES>(aj);
+      const float sc = sqrtf(ai * aj);
+      const bool cand = fabsf(gi) > 0.5f * kTol * sc && fabsf(aj - ai) <= kDegen * (ai + aj);
+      if (__any_sync(0xffffffffu, cand)) {
+        double g64 = 0.0;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r)
+          g64 = fma((double)As[i * CS + q * RPL + r], (double)As[j * CS + q * RPL + r], g64);
+        g64 = lanes_sum_d<LANES>(g64);
+        if (cand) {
+          ++fp64_tests;
+          if (fabs(g64) > (double)kTol * (double)sc) again = true;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  return __any_sync(0xffffffffu, again);
+}
+
+// Jacobi sweeps with the columns in registers: the round-robin moves them one
+// position per round.  Column norms are recomputed exactly at every sweep's
+// start and updated in closed form after each rotation.  Returns the sweeps
+// with rotations; As ([NC][CS]) stages the columns for the FP64 check.
+template <int RPL, int LANES, int NC, int CS, int U>
+__device__ int register_sweeps(RegCols<RPL, NC>& A, float* As, int q, int nwin,
+                               unsigned& fp64_tests) {
+  int sweeps = 0;
+  float nrm[NC];
+#pragma unroll 1
+  for (; sweeps < kMaxSweeps; ++sweeps) {
+#pragma unroll
+    for (int k = 0; k < NC - 1; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) s = fmaf(A(r, k), A(r, k), s);
+      nrm[k] = lanes_sum<LANES>(s);
+    }
+    nrm[NC - 1] = 0.f;
+    bool definite = false, band = false;
+#pragma unroll U
+    for (int rd = 0; rd < NC - 1; ++rd) {
+      float gm[NC / 2];
+#pragma unroll
+      for (int pp = 1; pp < NC / 2; ++pp) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) s = fmaf(A(r, pp), A(r, NC - 1 - pp), s);
+        gm[pp] = s;
+      }
+#pragma unroll
+      for (int o = 1; o < LANES; o <<= 1)
+#pragma unroll
+        for (int pp = 1; pp < NC / 2; ++pp) gm[pp] += __shfl_xor_sync(0xffffffffu, gm[pp], o);
+#pragma unroll
+      for (int pp = 1; pp < NC / 2; ++pp) {
+        const int pi = pp, pj = NC - 1 - pp;
+        const float al = nrm[pi], be = nrm[pj], gv = gm[pp];
+        const float g2 = gv * gv, ab = al * be;
+        const bool need = g2 > (kTol * kTol) * ab;
+        if (!__any_sync(0xffffffffu, need)) continue;  // converged pair in every lane
+        if (need) {
+          float cs, sn;
+          rotation(al, be, gv, g2, ab, cs, sn, definite, band);
+          A.rotate(pi, pj, cs, sn);
+          rotated_norms(al, be, gv, cs, sn, nrm[pi], nrm[pj]);
+        }
+      }
+      A.shift();
+      shift_norms<NC>(nrm);
+    }
+    if (__any_sync(0xffffffffu, definite)) continue;
+    if (!__any_sync(0xffffffffu, band)) break;
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) As[k * CS + q * RPL + r] = A(r, k);
+    __syncwarp();
+    if (!fp64_check<RPL, LANES, CS>(As, q, nwin, fp64_tests)) break;
+  }
+  return sweeps;
+}
+
 template <int RPL, int LANES, int NC, bool SM = false>
 __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
     k_svd(Problem pb, DeviceBuffers d, int nitems) {
@@ -277,96 +379,9 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
   // ---- Jacobi sweeps
   int sweeps = 0;
   unsigned fp64_tests = 0;
-  // Only near-degenerate pairs moved, by amounts at the FP32 noise level of
-  // their inner products: decide convergence from FP64 inner products of the
-  // current columns (exact products of the FP32 entries) staged in As.
-  auto fp64_again = [&]() {
-    bool again = false;
-    for (int i = 0; i < nwin; ++i) {
-      for (int j = i + 1; j < nwin; ++j) {
-        float gi = 0.f, ai = 0.f, aj = 0.f;
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) {
-          const float x = As[i * CS + q * RPL + r], y = As[j * CS + q * RPL + r];
-          gi = fmaf(x, y, gi);
-          ai = fmaf(x, x, ai);
-          aj = fmaf(y, y, aj);
-        }
-        gi = lanes_sum<LANES>(gi);
-        ai = lanes_sum<LANES>(ai);
-        aj = lanes_sum<LANES>(aj);
-        const float sc = sqrtf(ai * aj);
-        const bool cand = fabsf(gi) > 0.5f * kTol * sc && fabsf(aj - ai) <= kDegen * (ai + aj);
-        if (__any_sync(0xffffffffu, cand)) {
-          double g64 = 0.0;
-#pragma unroll
-          for (int r = 0; r < RPL; ++r)
-            g64 = fma((double)As[i * CS + q * RPL + r], (double)As[j * CS + q * RPL + r], g64);
-          g64 = lanes_sum_d<LANES>(g64);
-          if (cand) {
-            ++fp64_tests;
-            if (fabs(g64) > (double)kTol * (double)sc) again = true;
-          }
-        }
-      }
-    }
-    __syncwarp();
-    return __any_sync(0xffffffffu, again);
-  };
+  auto fp64_again = [&]() { return fp64_check<RPL, LANES, CS>(As, q, nwin, fp64_tests); };
   if constexpr (!SM) {
-    // columns in registers; the round-robin moves them one position per round
-    float nrm[NC];
-#pragma unroll 1
-    for (; sweeps < kMaxSweeps; ++sweeps) {
-#pragma unroll
-      for (int k = 0; k < NC - 1; ++k) {
-        float s = 0.f;
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) s = fmaf(A(r, k), A(r, k), s);
-        nrm[k] = lanes_sum<LANES>(s);
-      }
-      nrm[NC - 1] = 0.f;
-      bool definite = false, band = false;
-#pragma unroll U
-      for (int rd = 0; rd < NC - 1; ++rd) {
-        float gm[NC / 2];
-#pragma unroll
-        for (int pp = 1; pp < NC / 2; ++pp) {
-          float s = 0.f;
-#pragma unroll
-          for (int r = 0; r < RPL; ++r) s = fmaf(A(r, pp), A(r, NC - 1 - pp), s);
-          gm[pp] = s;
-        }
-#pragma unroll
-        for (int o = 1; o < LANES; o <<= 1)
-#pragma unroll
-          for (int pp = 1; pp < NC / 2; ++pp) gm[pp] += __shfl_xor_sync(0xffffffffu, gm[pp], o);
-#pragma unroll
-        for (int pp = 1; pp < NC / 2; ++pp) {
-          const int pi = pp, pj = NC - 1 - pp;
-          const float al = nrm[pi], be = nrm[pj], gv = gm[pp];
-          const float g2 = gv * gv, ab = al * be;
-          const bool need = g2 > (kTol * kTol) * ab;
-          if (!__any_sync(0xffffffffu, need)) continue;  // converged pair in every lane
-          if (need) {
-            float cs, sn;
-            rotation(al, be, gv, g2, ab, cs, sn, definite, band);
-            A.rotate(pi, pj, cs, sn);
-            rotated_norms(al, be, gv, cs, sn, nrm[pi], nrm[pj]);
-          }
-        }
-        A.shift();
-        shift_norms<NC>(nrm);
-      }
-      if (__any_sync(0xffffffffu, definite)) continue;
-      if (!__any_sync(0xffffffffu, band)) break;
-#pragma unroll
-      for (int k = 0; k < NC; ++k)
-#pragma unroll
-        for (int r = 0; r < RPL; ++r) As[k * CS + q * RPL + r] = A(r, k);
-      __syncwarp();
-      if (!fp64_again()) break;
-    }
+    sweeps = register_sweeps<RPL, LANES, NC, CS, U>(A, As, q, nwin, fp64_tests);
   } else {
     // columns in shared memory, addressed by the same round-robin schedule
     // (position k of round rd holds column (k + rd) mod (NC-1)): the same
@@ -528,7 +543,8 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
       for (int r = 0; r < RPL; ++r)
         if (roff[r] >= 0) d.U0[(((size_t)w * NCg + t) * g.M + q * RPL + r) * NP + p] = a[r];
     }
-    // v_t = B^T u_t / s_t and h_t = u_t^T G v_t, summed over the lanes' rows
+    // v_t = B^T u_t / s_t and h_t = u_t^T G v_t = sum_k v_k (G_k . u_t),
+    // the latter from the lanes' partial sums with one reduction
     float h = 0.f;
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
@@ -540,18 +556,17 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
       const float vk = bu * inv;
       if (c == 0 && live && use && (k % LANES) == q)
         d.V0[(((size_t)w * NCg + t) * nwin + k) * NP + p] = vk;
-      if (fw_) {
+      if (fw_ && live && use) {
+        const uint32_t pc = __ldg(posw + (size_t)k * g.P + posidx);
+        const size_t base = (size_t)k * F + (pc & 0xffffu) + (size_t)(pc >> 16) * g.S;
         float gu = 0.f;
-        if (live && use) {
-          const uint32_t pc = __ldg(posw + (size_t)k * g.P + posidx);
-          const size_t base = (size_t)k * F + (pc & 0xffffu) + (size_t)(pc >> 16) * g.S;
 #pragma unroll
-          for (int r = 0; r < RPL; ++r)
-            if (roff[r] >= 0) gu = fmaf(__ldg(fw_ + base + roff[r]), a[r], gu);
-        }
-        h = fmaf(vk, lanes_sum<LANES>(gu), h);
+        for (int r = 0; r < RPL; ++r)
+          if (roff[r] >= 0) gu = fmaf(__ldg(fw_ + base + roff[r]), a[r], gu);
+        h = fmaf(vk, gu, h);
       }
     }
+    if (fw_) h = lanes_sum<LANES>(h);
     if (live && use && q == 0) hvo[(size_t)t * NP] = h;
   }
 }

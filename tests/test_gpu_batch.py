@@ -103,7 +103,7 @@ def test_eight_rows_per_lane_shape_matches_oracle(capi, pkg, oracle, bs, T):
                 frame_begin=fr[0], frame_end=fr[1])
     Y0, _, st0 = capi.denoise(X, capi.default_params(autotune=0, **base))
     Y3, _, st3 = capi.denoise(X, capi.default_params(autotune=4, **base))
-    assert st0.svd_variant == 0 and st3.svd_variant == 3
+    assert st0.svd_variant == (4 if bs >= 7 else 0) and st3.svd_variant == 3
     Yo, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.5, block_size=bs,
                               traj_length=T, frame_begin=fr[0], frame_end=fr[1], n_jobs=2)
     f = slice(*fr)
@@ -122,6 +122,59 @@ def test_eight_rows_per_lane_shape_with_pgure(capi, pkg, oracle):
     np.testing.assert_allclose(e3[f], e0[f], rtol=2e-3)
     scale = np.abs(Y0[:, :, f]).max()
     assert np.abs(Y3[:, :, f] - Y0[:, :, f]).max() <= 1e-3 * scale
+
+
+@pytest.mark.parametrize("bs,T", [(5, 15), (6, 9), (8, 15), (8, 9), (7, 15)])
+def test_qr_preconditioned_shape_matches_oracle(capi, pkg, oracle, bs, T):
+    """Jacobi on the triangle of B's Householder QR factorisation (patches of
+    17..64 rows): right singular vectors from the sweeps, left ones from B."""
+    noisy, _, _ = pkg.synth.workload("arps_256", seed=10, side=40, nt=T + 2)
+    X = noisy.astype(np.float64)
+    fr = (T // 2, T // 2 + 2)
+    base = dict(median_size=0, optimize_pgure=0, lambda_=0.5, block_size=bs, traj_length=T,
+                frame_begin=fr[0], frame_end=fr[1])
+    Y0, _, st0 = capi.denoise(X, capi.default_params(autotune=0, **base))
+    Y4, _, st4 = capi.denoise(X, capi.default_params(autotune=5, **base))
+    # the untuned shape of 7x7 and 8x8 patches is the QR form itself
+    assert st0.svd_variant == (4 if bs >= 7 else 0) and st4.svd_variant == 4
+    Yo, _, _ = oracle.denoise(X, median_size=-1, optimize_pgure=0, lambda_=0.5, block_size=bs,
+                              traj_length=T, frame_begin=fr[0], frame_end=fr[1], n_jobs=2)
+    f = slice(*fr)
+    scale = np.abs(Yo[:, :, f]).max()
+    print("max relative difference to the oracle: QR form %.2e, default %.2e"
+          % (np.abs(Y4[:, :, f] - Yo[:, :, f]).max() / scale,
+             np.abs(Y0[:, :, f] - Yo[:, :, f]).max() / scale))
+    assert np.abs(Y4[:, :, f] - Yo[:, :, f]).max() <= 1e-4 * scale
+    assert np.abs(Y4[:, :, f] - Y0[:, :, f]).max() <= 1e-4 * scale
+
+
+def test_qr_preconditioned_shape_with_pgure(capi, pkg, oracle):
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=8, side=48, nt=18)
+    base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, frame_begin=6,
+                frame_end=10, block_size=8)
+    Y0, e0, _ = capi.denoise(noisy, capi.default_params(autotune=2, **base))  # 2 x 32 lanes
+    Y4, e4, st4 = capi.denoise(noisy, capi.default_params(autotune=5, **base))
+    assert st4.svd_variant == 4
+    f = slice(6, 10)
+    np.testing.assert_allclose(e4[f], e0[f], rtol=2e-3)
+    scale = np.abs(Y0[:, :, f]).max()
+    assert np.abs(Y4[:, :, f] - Y0[:, :, f]).max() <= 1e-3 * scale
+
+
+@pytest.mark.parametrize("bs,T", [(4, 9), (3, 7)])
+def test_two_kernel_register_form_is_identical(capi, pkg, bs, T):
+    """Patches of at most 16 rows run the register form's sweeps and its
+    factors in two kernels; the single-kernel shared-memory form applies the
+    same rotations in the same order: identical results."""
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=14, side=40, nt=T + 3)
+    base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, block_size=bs,
+                traj_length=T)
+    Y0, e0, st0 = capi.denoise(noisy, capi.default_params(autotune=0, **base))
+    Y2, e2, st2 = capi.denoise(noisy, capi.default_params(autotune=3, **base))
+    assert st0.svd_variant == 0 and st2.svd_variant == 2
+    np.testing.assert_array_equal(Y2, Y0)
+    np.testing.assert_array_equal(e2, e0)
+    assert st2.svd_warp_sweeps == st0.svd_warp_sweeps
 
 
 def test_shared_memory_svd_form_with_pgure(capi, pkg):
