@@ -403,7 +403,10 @@ def main():
     peaks = json.load(open(PEAKS_PATH)) if os.path.exists(PEAKS_PATH) else {}
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
-    roof = {"kernel": "k_svd (batched one-sided Jacobi, FP32 CUDA cores)", "bound": "fp32",
+    svd_kernels = {0: "k_bsweep + k_bout" if M <= 16 and N <= 15 else "k_svd",
+                   4: "k_qr + k_xsweep + k_qr_out"}.get(int(st.svd_variant), "k_svd")
+    roof = {"kernel": "SVD stage: %s (batched one-sided Jacobi, FP32 CUDA cores)" % svd_kernels,
+            "bound": "fp32",
             "achieved": svd_flop / svd_t / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": svd_flop / svd_t / 1e12 / fp32_peak,
             "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x 2 flop x %.0f MHz "
@@ -413,7 +416,7 @@ def main():
             "traffic": None}
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
-        roof["traffic"] = json.load(open(prof)).get("k_svd")
+        roof["traffic"] = json.load(open(prof)).get("svd_stage")
     # In the timed region the SVD of one window batch shares the GPU with the
     # other streams' lambda searches, so its event time overstates the
     # kernels' own.  The same launches alone: one batch of windows (the

@@ -202,17 +202,28 @@ __global__ void __launch_bounds__(128, 4) k_xsweep(Problem pb, DeviceBuffers d, 
   const int sweeps = register_sweeps<RX, 4, NC, CS, 1>(A, X, q, pb.g.nwin, fp64_tests);
   if (lane == 0) atomicAdd(d.counters + 1, (unsigned long long)(sweeps + 1));
   if (q == 0 && fp64_tests) atomicAdd(d.counters + 2, (unsigned long long)fp64_tests);
-  float* xo = d.xq + (size_t)(live ? gid : 0) * NC * D::XR;
+  // column norms (the singular values), then the rotated columns of those
+  // triplets that can survive the threshold (the only ones k_qr_out reads)
+  float sv[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
     float t = 0.f;
 #pragma unroll
-    for (int r = 0; r < RX; ++r) {
-      t = fmaf(A(r, k), A(r, k), t);
-      if (live) xo[k * D::XR + q * RX + r] = A(r, k);
-    }
-    t = lanes_sum<4>(t);  // every lane takes part
-    if (live && q == 0) d.xqn[(size_t)gid * NC + k] = sqrtf(t);
+    for (int r = 0; r < RX; ++r) t = fmaf(A(r, k), A(r, k), t);
+    sv[k] = sqrtf(lanes_sum<4>(t));  // every lane takes part
+  }
+  if (!live) return;
+  float smax = sv[0];
+#pragma unroll
+  for (int k = 1; k < NC; ++k) smax = fmaxf(smax, sv[k]);
+  const float upper = (float)d.wc[(gid / pb.g.NP) / d.ncopies].upper;
+  float* xo = d.xq + (size_t)gid * NC * D::XR;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    if (q == 0) d.xqn[(size_t)gid * NC + k] = sv[k];
+    if (can_survive(pb, sv[k], smax, upper))
+#pragma unroll
+      for (int r = 0; r < RX; ++r) xo[k * D::XR + q * RX + r] = A(r, k);
   }
 }
 
@@ -379,17 +390,28 @@ __global__ void __launch_bounds__(128, 4) k_bsweep(Problem pb, DeviceBuffers d, 
   const int sweeps = register_sweeps<RX, 4, NC, CS, 1>(A, X, q, nwin, fp64_tests);
   if (lane == 0) atomicAdd(d.counters + 1, (unsigned long long)(sweeps + 1));
   if (q == 0 && fp64_tests) atomicAdd(d.counters + 2, (unsigned long long)fp64_tests);
-  float* xo = d.xq + (size_t)(live ? gid : 0) * NC * XR;
+  // column norms (the singular values), then the rotated columns of those
+  // triplets that can survive the threshold (the only ones k_bout reads)
+  float sv[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
     float t = 0.f;
 #pragma unroll
-    for (int r = 0; r < RX; ++r) {
-      t = fmaf(A(r, k), A(r, k), t);
-      if (live) xo[k * XR + q * RX + r] = A(r, k);
-    }
-    t = lanes_sum<4>(t);  // every lane takes part
-    if (live && q == 0) d.xqn[(size_t)gid * NC + k] = sqrtf(t);
+    for (int r = 0; r < RX; ++r) t = fmaf(A(r, k), A(r, k), t);
+    sv[k] = sqrtf(lanes_sum<4>(t));  // every lane takes part
+  }
+  if (!live) return;
+  float smax = sv[0];
+#pragma unroll
+  for (int k = 1; k < NC; ++k) smax = fmaxf(smax, sv[k]);
+  const float upper = (float)d.wc[w].upper;
+  float* xo = d.xq + (size_t)gid * NC * XR;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    if (q == 0) d.xqn[(size_t)gid * NC + k] = sv[k];
+    if (can_survive(pb, sv[k], smax, upper))
+#pragma unroll
+      for (int r = 0; r < RX; ++r) xo[k * XR + q * RX + r] = A(r, k);
   }
 }
 
