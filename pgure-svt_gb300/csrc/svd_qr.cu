@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128, 4) k_bsweep(Problem pb, DeviceBuffers d, 
 }
 
 template <int NC>
-__global__ void __launch_bounds__(128) k_bout(Problem pb, DeviceBuffers d, int nitems) {
+__global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, int nitems) {
   constexpr int RX = 4, XR = 16;
   const Geometry& g = pb.g;
   const int lane = threadIdx.x & 31, q = lane & 3;
