@@ -336,8 +336,17 @@ struct Acc<unsigned long long> {  // 2^-32
 constexpr int kTileMax = 1024;     // pixels of a warp's shared-memory tile
 constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x 30 < 2048)
 
+// launch bounds of k_eval (a block is 32 x nwin threads, nwin <= 21)
+#ifndef PGSVT_EVAL_THREADS
+#define PGSVT_EVAL_THREADS (32 * 21)
+#endif
+#ifndef PGSVT_EVAL_MINB
+#define PGSVT_EVAL_MINB 1
+#endif
+
 template <int BS, typename AccT>
-__global__ void __launch_bounds__(32 * 21) k_eval(Problem pb, DeviceBuffers d, int final_pass) {
+__global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
+    k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   const int nb = BS > 0 ? BS : pb.g.bs;  // BS == 0: any side (9..16)
   const int M = nb * nb;
   constexpr int PB = kEvalPatches;  // patches per block
