@@ -28,6 +28,14 @@ class SVT:
     lambda_hint : float or None
         A proposed lambda (e.g. from the learned proposal): the search
         brackets it first and falls back to the full search.
+    learned_lambda : bool, default=False
+        Let the shipped learned model (lambda_mlp.npz) propose each
+        window's lambda; a narrow search around the proposal replaces the
+        plain search, which remains the fallback.
+    lambda_model : ndarray or None
+        A model of the same form to use instead of the shipped one.
+    autotune : int, default=0
+        SVD kernel shape selection (see include/pgsvt.h).
     """
 
     def __init__(self, trajectory_length=15, patch_size=4, patch_overlap=1,
@@ -36,7 +44,8 @@ class SVT:
                  noise_method=4, noise_alpha=None, noise_mu=None, noise_sigma=None,
                  tol=1e-7, max_iter=500, n_jobs=None, random_seed=None, *,
                  compat_flags=_capi.COMPAT_ALL, search_points=8, search_rounds=4,
-                 lambda_hint=None, window_batch=0, verbose=False):
+                 lambda_hint=None, window_batch=0, verbose=False, learned_lambda=False,
+                 lambda_model=None, autotune=0):
         self.trajectory_length = trajectory_length
         self.patch_size = patch_size
         self.patch_overlap = patch_overlap
@@ -60,7 +69,11 @@ class SVT:
         self.lambda_hint = lambda_hint
         self.window_batch = window_batch
         self.verbose = verbose
+        self.learned_lambda = learned_lambda
+        self.lambda_model = lambda_model
+        self.autotune = autotune
         self.Y_ = None
+        self._model = None
 
     def _check_arguments(self, X):
         """Sanity-checking of arguments (pguresvt/svt.py:212-271)."""
@@ -111,9 +124,27 @@ class SVT:
             if not _is_power_of_two(X.shape[0]):
                 raise ValueError("Quadtree noise estimation requires image dimensions 2^N")
 
+    def _model_array(self):
+        """The learned model in use (kept alive on the estimator), or None."""
+        if self.lambda_model is not None:
+            m = np.ascontiguousarray(self.lambda_model, dtype=np.float32)
+        elif self.learned_lambda:
+            from . import learned
+            m = learned.load_model()
+        else:
+            return None
+        if m.size != _capi.LAMBDA_MODEL_FLOATS:
+            raise ValueError("lambda model has %d floats, expected %d"
+                             % (m.size, _capi.LAMBDA_MODEL_FLOATS))
+        self._model = m
+        return m
+
     def params(self):
         """The pgsvt_params this estimator passes to the library."""
+        model = self._model_array()
         return _capi.default_params(
+            lambda_model=0 if model is None else model.ctypes.data,
+            autotune=int(self.autotune),
             traj_length=self.trajectory_length, block_size=self.patch_size,
             block_overlap=self.patch_overlap, motion_window=self.motion_window,
             median_size=self.motion_filter_, noise_method=self.noise_method,

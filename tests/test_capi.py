@@ -52,6 +52,24 @@ def test_lambda_model_constants(capi):
     assert capi.LAMBDA_MODEL_FLOATS == 2 * F + capi.LAMBDA_PARAMS + 2
 
 
+def test_svt_learned_lambda_parameters(pkg, capi):
+    """The SVT shim's keyword-only extras: the shipped (or a given) learned
+    model and the SVD shape selection reach pgsvt_params."""
+    X = np.ones((32, 32, 16))
+    s = pkg.SVT(learned_lambda=True, autotune=1)
+    s._check_arguments(X)
+    p = s.params()
+    assert p.lambda_model and p.autotune == 1
+    assert s._model.dtype == np.float32 and s._model.size == capi.LAMBDA_MODEL_FLOATS
+    s = pkg.SVT()
+    s._check_arguments(X)
+    assert not s.params().lambda_model
+    s = pkg.SVT(lambda_model=np.zeros(10, np.float32))
+    s._check_arguments(X)
+    with pytest.raises(ValueError, match="lambda model has 10 floats"):
+        s.params()
+
+
 class TestErrors:
     """pguresvt/tests/test_svt.py:109-164: validation happens before any call."""
 

@@ -191,6 +191,24 @@ def test_svt_estimator_on_gpu(pkg, g):
     assert np.all(s.lambda1s_ > 0) and np.all(s.noise_alphas_ == float(g["alpha"]))
 
 
+def test_svt_estimator_with_learned_lambda(pkg):
+    """The shim with the shipped learned proposal, on the reference's default
+    path (median pre-filter 5, noise estimated): fewer risk evaluations than
+    the plain search, the same output to within the risk gap's effect."""
+    clean = pkg.synth.blobs(64, 20, 12, seed=5) * 40.0
+    rng = np.random.RandomState(7)
+    Y = np.maximum(clean + 5.0 + 4.0 * rng.randn(*clean.shape), 0.0).astype(np.uint16)
+    plain = pkg.SVT(random_seed=7).denoise(Y)
+    learned = pkg.SVT(random_seed=7, learned_lambda=True).denoise(Y)
+    print("risk evaluations plain %d learned %d" % (plain.status_.risk_evals,
+                                                    learned.status_.risk_evals))
+    assert learned.status_.risk_evals < plain.status_.risk_evals
+    assert np.all(np.isfinite(learned.lambda1s_)) and np.all(learned.lambda1s_ >= 0)
+    err = np.abs(learned.Y_ - plain.Y_).max() / np.abs(plain.Y_).max()
+    print("max relative output difference", err)
+    assert err < 0.05
+
+
 def test_errors(capi, pkg):
     X = np.ones((16, 16, 16), np.float32)
     p = capi.default_params(median_size=-1, optimize_pgure=0, lambda_=0.1)
