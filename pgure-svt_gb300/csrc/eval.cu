@@ -346,7 +346,7 @@ constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x
 
 template <int BS, typename AccT>
 __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
-    k_eval(Problem pb, DeviceBuffers d, int final_pass) {
+    k_eval(Problem pb, DeviceBuffers d, int final_pass, int stage) {
   const int nb = BS > 0 ? BS : pb.g.bs;  // BS == 0: any side (9..16)
   const int M = nb * nb;
   constexpr int PB = kEvalPatches;  // patches per block
@@ -402,6 +402,23 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
     }
   }
   __syncthreads();
+  // patches of at most 16 rows: the left singular vectors of the block's
+  // patches, up to the largest rank any lambda of the round keeps, staged in
+  // shared memory once ([i][e][PB]); every slice warp and every lambda reads
+  // them there instead of through L1
+  constexpr bool kStage = BS > 0 && BS * BS <= 16;
+  float* Us = (float*)(tiles + (size_t)nwarps * kTileMax);
+  if (kStage && stage) {  // uniform over the block
+    int R = 0;
+    for (int j = 0; j < nl; ++j) R = max(R, srmax[j]);
+    const float* U0w = d.U0 + (size_t)w * NC * M * NP;
+    for (int t = threadIdx.x; t < R * M * PB; t += blockDim.x) {
+      const int slot = t % PB, ie = t / PB;  // ie = i * M + e
+      const int p = blockIdx.x * PB + slot;
+      Us[t] = p < g.NP ? __ldg(U0w + (size_t)ie * NP + p) : 0.f;
+    }
+    __syncthreads();
+  }
   if (lin_terms)
     for (int j = k; j < nl; j += nwarps) {
       float lin = 0.f;
@@ -460,10 +477,17 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
           const float coef = sg[((size_t)j * NC + i) * PB + h * 32 + lane] *
                              V0[((size_t)i * g.nwin + k) * NP + p];
           if (coef == 0.f) continue;
-          const float* ui = U0 + ((size_t)i * M + e0) * NP + p;
+          if (kStage && stage) {
+            const float* ui = Us + ((size_t)i * M + e0) * PB + h * 32 + lane;
 #pragma unroll
-          for (int e = 0; e < CH; ++e)
-            if (e0 + e < M) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
+            for (int e = 0; e < CH; ++e)
+              if (e0 + e < M) col[e] = fmaf(coef, ui[e * PB], col[e]);
+          } else {
+            const float* ui = U0 + ((size_t)i * M + e0) * NP + p;
+#pragma unroll
+            for (int e = 0; e < CH; ++e)
+              if (e0 + e < M) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
+          }
         }
 #pragma unroll
         for (int e = 0; e < CH; ++e) {
@@ -614,40 +638,46 @@ __global__ void k_risk_collect(Problem pb, DeviceBuffers d, double* out) {
   }
 }
 
-size_t eval_smem(const Geometry& g, int nl) {
-  return (size_t)nl * (g.NC + 4) * kEvalPatches * sizeof(float) +
-         (size_t)g.nwin * kTileMax * sizeof(int);
+// shared memory of a k_eval block; stage: the left vectors fit beside it
+size_t eval_smem(const Geometry& g, int nl, int& stage) {
+  const size_t base = (size_t)nl * (g.NC + 4) * kEvalPatches * sizeof(float) +
+                      (size_t)g.nwin * kTileMax * sizeof(int);
+  const size_t staged = g.bs <= 4 ? (size_t)g.NC * g.M * kEvalPatches * sizeof(float) : 0;
+  stage = (staged > 0 && base + staged <= 227 * 1024) ? 1 : 0;
+  return base + (stage ? staged : 0);
 }
 
 template <int BS, typename AccT>
 void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const Problem& pb,
-                      const DeviceBuffers& d, int final_pass) {
+                      const DeviceBuffers& d, int final_pass, int stage) {
   cudaFuncSetAttribute(k_eval<BS, AccT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass);
+  k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass, stage);
 }
 
 template <typename AccT>
 void launch_k_eval_t(int bs, dim3 grid, int threads, size_t shm, cudaStream_t s,
-                     const Problem& pb, const DeviceBuffers& d, int final_pass) {
+                     const Problem& pb, const DeviceBuffers& d, int final_pass, int stage) {
   switch (bs) {
-    case 2: launch_k_eval_bs<2, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 3: launch_k_eval_bs<3, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 4: launch_k_eval_bs<4, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 5: launch_k_eval_bs<5, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 6: launch_k_eval_bs<6, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 7: launch_k_eval_bs<7, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    case 8: launch_k_eval_bs<8, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
-    default: launch_k_eval_bs<0, AccT>(grid, threads, shm, s, pb, d, final_pass); break;
+    case 2: launch_k_eval_bs<2, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 3: launch_k_eval_bs<3, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 4: launch_k_eval_bs<4, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 5: launch_k_eval_bs<5, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 6: launch_k_eval_bs<6, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 7: launch_k_eval_bs<7, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    case 8: launch_k_eval_bs<8, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
+    default: launch_k_eval_bs<0, AccT>(grid, threads, shm, s, pb, d, final_pass, stage); break;
   }
 }
 
 void launch_k_eval(const Problem& pb, const DeviceBuffers& d, int final_pass, int nl,
                    cudaStream_t s) {
   const Geometry& g = pb.g;
-  const size_t shm = eval_smem(g, nl);
+  int stage = 0;
+  const size_t shm = eval_smem(g, nl, stage);
   const dim3 grid(d.nblk_eval, pb.W);
-  if (pb.acc64) launch_k_eval_t<unsigned long long>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass);
-  else launch_k_eval_t<int>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass);
+  if (pb.acc64)
+    launch_k_eval_t<unsigned long long>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass, stage);
+  else launch_k_eval_t<int>(g.bs, grid, 32 * g.nwin, shm, s, pb, d, final_pass, stage);
 }
 
 void launch_k_mse(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {

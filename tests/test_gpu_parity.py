@@ -195,9 +195,8 @@ def test_svt_estimator_with_learned_lambda(pkg):
     """The shim with the shipped learned proposal, on the reference's default
     path (median pre-filter 5, noise estimated): fewer risk evaluations than
     the plain search, the same output to within the risk gap's effect."""
-    clean = pkg.synth.blobs(64, 20, 12, seed=5) * 40.0
-    rng = np.random.RandomState(7)
-    Y = np.maximum(clean + 5.0 + 4.0 * rng.randn(*clean.shape), 0.0).astype(np.uint16)
+    Y, noise = pkg.learned.random_sequence(10 ** 7 + 200, estimated=True)  # held out
+    assert noise is None
     plain = pkg.SVT(random_seed=7).denoise(Y)
     learned = pkg.SVT(random_seed=7, learned_lambda=True).denoise(Y)
     print("risk evaluations plain %d learned %d" % (plain.status_.risk_evals,
