@@ -326,7 +326,9 @@ def main():
 
     # ---- learned-lambda form: the shipped MLP's proposal + narrow search
     learned = None
-    if not args.no_learned:
+    if not args.no_learned and args.patch != 4:
+        learned = {"skipped": "the shipped lambda model covers 4x4 patches and 15-frame windows"}
+    elif not args.no_learned:
         model = pkg.learned.load_model()
         pl = params(capi, a, m, s, args.patch, -1.0, args.autotune)
         pl.lambda_model = model.ctypes.data
@@ -490,7 +492,7 @@ def main():
                                                            est.cpu().numpy().reshape(4, nimg)[1:, 0]],
                                 "config": "median filter 5, alpha/mu/sigma estimated "
                                           "(noise method 4), PGURE on, same sequence"}
-        if not args.no_learned:  # the learned proposal on the default path
+        if not args.no_learned and args.patch == 4:  # the learned proposal on the default path
             model = pkg.learned.load_model()
             pd.lambda_model = model.ctypes.data
             lms = timed_once(pd)

@@ -102,7 +102,9 @@ typedef struct {
   uint32_t frame_end;       /* computed (0,0: all); others are left zero  */
   /* Learned lambda proposal (not in the reference): a host array of
    * PGSVT_LAMBDA_MODEL_FLOATS floats (see pgsvt_lambda_train), NULL: off.
-   * Each window's proposal replaces lambda_hint for that window.           */
+   * Each window's proposal replaces lambda_hint for that window.  A model
+   * serves the patch size and window length it was trained on: the shipped
+   * one (lambda_mlp.npz) covers 4x4 patches and 15-frame windows.          */
   const float* lambda_model;
   uint32_t hint_points;     /* lambda values per narrow-search round (0: 4) */
   uint32_t hint_rounds;     /* refinement rounds of the narrow search (0: 1) */

@@ -29,9 +29,10 @@ class SVT:
         A proposed lambda (e.g. from the learned proposal): the search
         brackets it first and falls back to the full search.
     learned_lambda : bool, default=False
-        Let the shipped learned model (lambda_mlp.npz) propose each
-        window's lambda; a narrow search around the proposal replaces the
-        plain search, which remains the fallback.
+        Let the shipped learned model (lambda_mlp.npz, trained for 4x4
+        patches and 15-frame trajectories) propose each window's lambda; a
+        narrow search around the proposal replaces the plain search, which
+        remains the fallback.
     lambda_model : ndarray or None
         A model of the same form to use instead of the shipped one.
     autotune : int, default=0
@@ -130,6 +131,9 @@ class SVT:
             m = np.ascontiguousarray(self.lambda_model, dtype=np.float32)
         elif self.learned_lambda:
             from . import learned
+            if self.patch_size != 4 or self.trajectory_length != 15:
+                raise ValueError("the shipped lambda model covers patch_size 4 and "
+                                 "trajectory_length 15; pass lambda_model= for others")
             m = learned.load_model()
         else:
             return None

@@ -68,6 +68,10 @@ def test_svt_learned_lambda_parameters(pkg, capi):
     s._check_arguments(X)
     with pytest.raises(ValueError, match="lambda model has 10 floats"):
         s.params()
+    s = pkg.SVT(learned_lambda=True, patch_size=8)  # outside the shipped model's range
+    s._check_arguments(X)
+    with pytest.raises(ValueError, match="covers patch_size 4"):
+        s.params()
 
 
 class TestErrors:
