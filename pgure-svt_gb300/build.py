@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpgsvt.so")
 SOURCES = ["prep.cu", "arps.cu", "svd.cu", "svd_i0.cu", "svd_i1.cu", "svd_i2.cu", "svd_i3.cu",
-           "svd_i4.cu", "svd_i5.cu", "svd_i6.cu", "svd_i7.cu", "svd_i8.cu", "svd_qr.cu", "svd_s0.cu", "svd_s1.cu",
+           "svd_i4.cu", "svd_i5.cu", "svd_i6.cu", "svd_i7.cu", "svd_i8.cu", "svd_split.cu", "svd_s0.cu", "svd_s1.cu",
            "svd_s2.cu", "svd_s3.cu", "svd_s4.cu", "eval.cu", "lambda.cu", "noise.cu", "hotpixel.cu",
            "capi.cu", "noalloc.cu"]
 CLI_SRC = os.path.join(HERE, "cli", "pgsvt_cli.cpp")

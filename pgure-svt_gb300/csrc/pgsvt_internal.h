@@ -157,7 +157,7 @@ struct DeviceBuffers {
   float* V0;
   float* sv;
   float* hv;
-  float* xq;               // split SVD forms' scratch: [items][NC][X rows] (svd_qr.cu)
+  float* xq;               // split SVD forms' scratch: [items][NC][X rows] (svd_split.cu)
   float* xqn;              // its column norms [items][NC]
   int32_t* nlive0;         // [W][NP] singular triplets of copy 0 that can survive
   void* acc;               // [W][K][nwin][S*S] int32 or int64 fixed point

@@ -55,9 +55,9 @@ bool svd_supported(int bs, int nwin) {
 // per-pair rotation arithmetic, replicated in every lane of a patch, is shared
 // by twice the rows; 2 resident blocks per SM instead of 3), variant 4
 // (patches of 17..64 rows, windows <= 15) sweeps the triangle of B's QR
-// factorisation instead of B (svd_qr.cu).  For patches of at most 16 rows
+// factorisation instead of B (svd_split.cu).  For patches of at most 16 rows
 // and windows of at most 15 frames variant 0 runs its sweeps and its factors
-// in two kernels (svd_qr.cu; the sweeps without the factors' registers fit
+// in two kernels (svd_split.cu; the sweeps without the factors' registers fit
 // four resident blocks per SM instead of three), with identical results,
 // wherever the caller provides the scratch (not in the allocation-free entry).  Variants 0 and 2 apply the same
 // rotations in the same order; all agree to FP32 rounding.  The autotuner

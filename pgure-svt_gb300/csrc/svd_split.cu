@@ -1,24 +1,29 @@
-// svd_qr.cu — QR-preconditioned Jacobi SVD for Casorati matrices of 17..64
-// rows (patch sides 5..8) and windows of up to 15 frames.
+// svd_split.cu — SVD forms that run as several kernels, each with a small
+// code footprint (one kernel holding all phases thrashed the instruction
+// cache) and its own register budget:
 //
-// A one-sided Jacobi sweep costs work proportional to the rows of the
-// matrix it orthogonalises.  For an m x n Casorati matrix B with m > n the
-// kernel first reduces B to the n x n triangle R of its Householder QR
-// factorisation (B = Q R), then runs the Jacobi sweeps on X = R^T, whose
-// rotated columns X W = U_X S give the right singular vectors of B directly
-// (R = W S U_X^T, so B = (Q W) S U_X^T): v_t = U_X e_t, and the left ones
-// follow from B itself, u_t = B v_t / s_t.  Q and W are never formed.
-//
-// Three kernels, each with a small code footprint (one kernel holding all
-// three phases thrashed the instruction cache):
+// QR-preconditioned form, Casorati matrices of 17..64 rows (patch sides
+// 5..8) and windows of up to 15 frames.  A one-sided Jacobi sweep costs work
+// proportional to the rows of the matrix it orthogonalises.  For an m x n
+// Casorati matrix B with m > n the kernels first reduce B to the n x n
+// triangle R of its Householder QR factorisation (B = Q R), then run the
+// Jacobi sweeps on X = R^T, whose rotated columns X W = U_X S give the right
+// singular vectors of B directly (R = W S U_X^T, so B = (Q W) S U_X^T):
+// v_t = U_X e_t, and the left ones follow from B itself, u_t = B v_t / s_t.
+// Q and W are never formed.
 //   k_qr      16 lanes per patch: B staged in shared memory, Householder
 //             reflections in a runtime loop; X = R^T to a scratch array
 //   k_xsweep  4 lanes x (NC/4) rows per patch, eight patches per warp: the
 //             register-form Jacobi sweeps of svd_kernel.cuh (same rotations,
-//             same convergence rules) on X; rotated X and its column norms
+//             same convergence rules) on X; rotated columns and their norms
 //             back to the scratch
 //   k_qr_out  16 lanes x 4 rows per patch: u_t = B v_t / s_t, the stored
 //             factors and the risk projections h_t = u_t^T G v_t.
+//
+// Two-kernel register form, at most 16 rows and windows of up to 15 frames
+// (the default for patch sides 2..4): k_bsweep runs the register form's
+// sweeps on B at four resident blocks per SM, k_bout the factors, exactly as
+// the single-kernel form computes them.
 #include "svd_kernel.cuh"
 
 namespace pgsvt {
