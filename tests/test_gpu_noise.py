@@ -35,6 +35,20 @@ def test_estimates_match_frozen_oracle(capi, method):
         np.testing.assert_allclose(est[:, 1:], np.tile(ref, (T, 1)), rtol=1e-4)
 
 
+@pytest.mark.parametrize("method", [1, 2, 3, 4])
+def test_estimates_of_a_flat_short_window(capi, oracle, method):
+    """A flat 5-frame window (one leaf per frame): method 1's leaf count is
+    clamped to the leaves on both sides."""
+    rng = np.random.default_rng(0)
+    u = np.asfortranarray(0.5 + 1e-3 * rng.standard_normal((32, 32, 5)))
+    u /= u.max()
+    p = capi.default_params(median_size=0, traj_length=5, noise_method=method,
+                            random_seed=3, search_points=4, search_rounds=1)
+    _, est, _ = capi.denoise(u, p)
+    ref = oracle.noise_estimate(u, method=method)
+    np.testing.assert_allclose(est[:, 1:], np.tile(ref, (5, 1)), rtol=1e-4)
+
+
 def test_estimates_match_live_oracle(capi, pkg, oracle):
     noisy, _, _ = pkg.synth.workload("arps_256", seed=21, side=64, nt=18)
     X = noisy.astype(np.float64)

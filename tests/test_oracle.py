@@ -282,6 +282,21 @@ def test_noise_estimator_frozen(oracle):
             np.testing.assert_allclose(est, z["est_%d" % k][method - 1], rtol=1e-12)
 
 
+def test_noise_method1_leaf_count_is_clamped(oracle):
+    """Method 1 takes the first round(0.05 * floor(Nx Ny / leaves)) + 1 leaves
+    in mean order (noise.hpp:115-123).  On a flat window of few frames each
+    frame is one leaf, and that count exceeds the leaves (where the reference
+    reads past its arrays): the restatement takes every leaf instead, so mu
+    is the mode of all leaf means, as method 2 computes it."""
+    rng = np.random.default_rng(0)
+    u = np.asfortranarray(0.5 + 1e-3 * rng.standard_normal((32, 32, 5)))
+    u /= u.max()
+    e1 = oracle.noise_estimate(u, method=1)
+    e2 = oracle.noise_estimate(u, method=2)
+    assert np.all(np.isfinite(e1)) and e1[1] > 0 and e1[2] > 0
+    assert e1[0] == e2[0] and e1[1] == e2[1]
+
+
 def test_noise_estimator_keeps_given_values(oracle):
     z = np.load(os.path.join(GOLDEN, "noise.npz"))
     a, m, s = oracle.noise_estimate(z["u_0"], alpha=0.5, mu=-1, sigma=0.25)
