@@ -465,6 +465,10 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
   const float* fw_ = (pb.optimize && fld) ? fld + (size_t)w * g.cube() : nullptr;
   PatchSrc src;
   src.init(pb, d, p, c, w);
+  // B again and, in shared memory, this lane's rows of the field G along the
+  // trajectory (each lane reads back only what it wrote)
+  __shared__ __align__(16) float Gs[32][NC][4 * RX];
+  float* gs = &Gs[threadIdx.x >> 2][0][q * RX];
   float B[RX][NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
@@ -472,6 +476,14 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
     const size_t b = colok ? src.base(k) : 0;
 #pragma unroll
     for (int r = 0; r < RX; ++r) B[r][k] = (colok && roff[r] >= 0) ? src.value(b + roff[r]) : 0.f;
+    if (fw_) {
+      float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      float* gp = &g4.x;
+#pragma unroll
+      for (int r = 0; r < RX; ++r)
+        if (colok && roff[r] >= 0) gp[r] = __ldg(fw_ + b + roff[r]);
+      *reinterpret_cast<float4*>(gs + k * 4 * RX) = g4;
+    }
   }
   int prev = -1;
   float prev_s = INFINITY;
@@ -518,11 +530,12 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
       if (c == 0 && live && use && (k % 4) == q)
         d.V0[(((size_t)w * NCg + t) * nwin + k) * NP + p] = vk;
       if (fw_ && live && use) {
-        const size_t base = src.base(k);
+        const float4 g4 = *reinterpret_cast<const float4*>(gs + k * 4 * RX);
+        const float* gp = &g4.x;
         float gu = 0.f;
 #pragma unroll
         for (int r = 0; r < RX; ++r)
-          if (roff[r] >= 0) gu = fmaf(__ldg(fw_ + base + roff[r]), a[r], gu);
+          if (roff[r] >= 0) gu = fmaf(gp[r], a[r], gu);
         h = fmaf(vk, gu, h);
       }
     }
