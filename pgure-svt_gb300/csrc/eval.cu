@@ -344,9 +344,9 @@ constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x
 #define PGSVT_EVAL_MINB 1
 #endif
 
-template <int BS, typename AccT>
+template <int BS, typename AccT, bool STAGE = false>
 __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
-    k_eval(Problem pb, DeviceBuffers d, int final_pass, int stage) {
+    k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   const int nb = BS > 0 ? BS : pb.g.bs;  // BS == 0: any side (9..16)
   const int M = nb * nb;
   constexpr int PB = kEvalPatches;  // patches per block
@@ -406,9 +406,9 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
   // patches, up to the largest rank any lambda of the round keeps, staged in
   // shared memory once ([i][e][PB]); every slice warp and every lambda reads
   // them there instead of through L1
-  constexpr bool kStage = BS > 0 && BS * BS <= 16;
+  constexpr bool kStage = STAGE && BS > 0 && BS * BS <= 16;
   float* Us = (float*)(tiles + (size_t)nwarps * kTileMax);
-  if (kStage && stage) {  // uniform over the block
+  if constexpr (kStage) {
     int R = 0;
     for (int j = 0; j < nl; ++j) R = max(R, srmax[j]);
     const float* U0w = d.U0 + (size_t)w * NC * M * NP;
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
           const float coef = sg[((size_t)j * NC + i) * PB + h * 32 + lane] *
                              V0[((size_t)i * g.nwin + k) * NP + p];
           if (coef == 0.f) continue;
-          if (kStage && stage) {
+          if constexpr (kStage) {
             const float* ui = Us + ((size_t)i * M + e0) * PB + h * 32 + lane;
 #pragma unroll
             for (int e = 0; e < CH; ++e)
@@ -650,8 +650,16 @@ size_t eval_smem(const Geometry& g, int nl, int& stage) {
 template <int BS, typename AccT>
 void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const Problem& pb,
                       const DeviceBuffers& d, int final_pass, int stage) {
+  if constexpr (BS > 0 && BS * BS <= 16) {
+    if (stage) {  // the left vectors staged in shared memory
+      cudaFuncSetAttribute(k_eval<BS, AccT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)shm);
+      k_eval<BS, AccT, true><<<grid, threads, shm, s>>>(pb, d, final_pass);
+      return;
+    }
+  }
   cudaFuncSetAttribute(k_eval<BS, AccT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass, stage);
+  k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass);
 }
 
 template <typename AccT>
