@@ -491,7 +491,8 @@ def main():
                                 "noise_estimates_frame0": [float(v) for v in
                                                            est.cpu().numpy().reshape(4, nimg)[1:, 0]],
                                 "config": "median filter 5, alpha/mu/sigma estimated "
-                                          "(noise method 4), PGURE on, same sequence"}
+                                          "(noise method 4), PGURE on, same sequence"
+                                          + ("; rank 0 alone" if world > 1 else "")}
         if not args.no_learned and args.patch == 4:  # the learned proposal on the default path
             model = pkg.learned.load_model()
             pd.lambda_model = model.ctypes.data
@@ -505,7 +506,7 @@ def main():
                 "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
     if args.batch:
         line["batch"] = run_batch(capi, args.batch, args.seed, full=args.batch_full)
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the CPU baseline: rank 0 at N = 1 only
         threads = os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(noisy, (a, m, s), args.patch, evals_per_window,
                                             args.cpu_stride or choose_stride(S, args.patch),
