@@ -356,7 +356,9 @@ int pgsvt_hot_pixel_filter(uint16_t* frames, uint32_t nrows, uint32_t ncols, uin
  * are limited to nrows <= PGSVT_NOALLOC_MAX_SIDE, nwin <= PGSVT_NOALLOC_MAX_NWIN
  * and block_size <= 4; larger ones are rejected with PGSVT_ERR_INVALID_ARG.
  * The first call on a device looks up that device's copy of the array (make
- * it before any stream capture).  All calls share the array and it keeps the
+ * it before any stream capture); the first call after a cudaDeviceReset
+ * looks it up again.  Non-finite or huge pixel values give non-finite
+ * singular values, never a fault.  All calls share the array and it keeps the
  * previous call's contents: calls whose GPU work overlaps race, so serialise
  * them.  Runs on `stream` (a cudaStream_t, NULL: default stream) and returns
  * once the work has completed.  Calls no allocating routine.                */

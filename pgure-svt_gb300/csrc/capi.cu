@@ -96,20 +96,7 @@ void make_probes(int64_t seed, size_t n, int8_t* d1, int8_t* d2code) {
 }
 
 // ---------------------------------------------------------------------------
-// Kept patches (svt.hpp:61-94): the row-major-looking index i*nyMbs + j of the
-// first loop is reproduced as written, then the right and bottom edges are
-// added and the set is sorted and made unique.
-std::vector<int32_t> patch_list(int S, int bs, int ov) {
-  const int64_t nMbs = S - bs;
-  std::vector<int64_t> v;
-  for (int64_t i = 0; i < 1 + nMbs; i += ov)
-    for (int64_t j = 0; j < 1 + nMbs; j += ov) v.push_back(i * nMbs + j);
-  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * i + nMbs);
-  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * nMbs + i);
-  std::sort(v.begin(), v.end());
-  v.erase(std::unique(v.begin(), v.end()), v.end());
-  return std::vector<int32_t>(v.begin(), v.end());
-}
+std::vector<int32_t> patch_list(int S, int bs, int ov) { return kept_patches(S, bs, ov); }
 
 // Processing order of the kept patches: 8 x 8 tiles of grid positions (rows
 // fastest), so the 64 patches of a lambda-evaluation block cover a compact

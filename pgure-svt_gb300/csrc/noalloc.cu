@@ -12,7 +12,10 @@
 // rejected.  All calls share the array, which keeps the last call's contents;
 // calls whose GPU work overlaps (other host threads, other streams) race on
 // it and must be serialised by the caller.
+#include <cuda.h>
+
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -67,7 +70,37 @@ __global__ void k_export_sv(const float* sv, int NP, int NC, int nwin, float* S)
 }
 
 std::mutex g_mu;
-void* g_addr[64];  // scratch address per device, resolved on first use
+void* g_addr[64];                // scratch address per device, resolved on first use ...
+unsigned long long g_ctx[64];    // ... in the context with this identifier
+
+// Identifier of the calling thread's current CUDA context (0: none yet).  A
+// device reset destroys the context that held the scratch and a new one gets
+// a new identifier, so the address is resolved again after a reset.  The
+// driver entry points are looked up through the runtime (no libcuda link).
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 int fail(int code, const std::string& m) {
   set_last_error(m);  // read back with pgsvt_last_error()
@@ -99,16 +132,19 @@ extern "C" int pgsvt_svd_window_noalloc(const float* u_dev, uint32_t nrows, uint
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
     return fail(PGSVT_ERR_CUDA, "no usable CUDA device");
   // one-time set-up per device (the device is current): the host-side name
-  // g_scratch is not a device address, ask the runtime for it
+  // g_scratch is not a device address, ask the runtime for it; again when the
+  // device's context has changed since (after a cudaDeviceReset)
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_addr[dev] || ctx == 0 || ctx != g_ctx[dev]) {
       const cudaError_t e = cudaGetSymbolAddress(&g_addr[dev], g_scratch);
       if (e != cudaSuccess) {
         g_addr[dev] = nullptr;
         return fail(PGSVT_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       }
+      g_ctx[dev] = current_context_id();  // the set-up made the context current
     }
     base = g_addr[dev];
   }
@@ -127,18 +163,7 @@ extern "C" int pgsvt_svd_window_noalloc(const float* u_dev, uint32_t nrows, uint
   g.NC = svd_columns(g.nwin);
   g.mw = 0;
   g.nimg = g.nwin;
-  std::vector<int32_t> plist;
-  {
-    const int64_t nMbs = g.S - g.bs, ov = block_overlap;
-    std::vector<int64_t> v;  // svt.hpp:61-94
-    for (int64_t i = 0; i < 1 + nMbs; i += ov)
-      for (int64_t j = 0; j < 1 + nMbs; j += ov) v.push_back(i * nMbs + j);
-    for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * i + nMbs);
-    for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * nMbs + i);
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-    plist.assign(v.begin(), v.end());
-  }
+  const std::vector<int32_t> plist = kept_patches(g.S, g.bs, (int)block_overlap);
   g.NP = (int)plist.size();
   *npatch = (uint32_t)g.NP;
   if (!S_dev) return PGSVT_OK;  // size query
@@ -147,9 +172,9 @@ extern "C" int pgsvt_svd_window_noalloc(const float* u_dev, uint32_t nrows, uint
   pb.g = g;
   pb.W = 1;
   pb.K = 1;
-  pb.optimize = 0;     // singular values only: a flat threshold above every singular
-  pb.expw = 0;         // value keeps no triplet, so no U/V factors are written
-  pb.lambda_user = 1e30;
+  pb.optimize = 0;     // singular values only: an infinite flat threshold keeps no
+  pb.expw = 0;         // triplet (not even an infinite singular value), so no
+  pb.lambda_user = INFINITY;  // U/V factors are written (d.U0, d.V0 stay null)
   pb.compat = PGSVT_COMPAT_ALL;
   DeviceBuffers d{};
   d.u = const_cast<float*>(u_dev);

@@ -30,9 +30,27 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
+#include <vector>
 
 namespace pgsvt {
+
+// Kept patches (svt.hpp:61-94): the row-major-looking index i*nyMbs + j of the
+// first loop is reproduced as written, then the right and bottom edges are
+// added and the set is sorted and made unique.  Every entry point builds its
+// patch list here, so all of them keep the same patches in the same order.
+inline std::vector<int32_t> kept_patches(int S, int bs, int ov) {
+  const int64_t nMbs = S - bs;
+  std::vector<int64_t> v;
+  for (int64_t i = 0; i < 1 + nMbs; i += ov)
+    for (int64_t j = 0; j < 1 + nMbs; j += ov) v.push_back(i * nMbs + j);
+  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * i + nMbs);
+  for (int64_t i = 0; i < 1 + nMbs; i += ov) v.push_back((nMbs + 1) * nMbs + i);
+  std::sort(v.begin(), v.end());
+  v.erase(std::unique(v.begin(), v.end()), v.end());
+  return std::vector<int32_t>(v.begin(), v.end());
+}
 
 constexpr int kMaxK = 16;          // lambda values per evaluation round
 constexpr int kMaxPts = 160;       // evaluated points kept per window

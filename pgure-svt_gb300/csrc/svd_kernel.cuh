@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
     float a[RPL];
 #pragma unroll
     for (int r = 0; r < RPL; ++r) a[r] = As[ct * CS + q * RPL + r] * inv;  // u_t rows
-    if (c == 0 && live && use) {
+    if (c == 0 && live && use && d.U0) {
 #pragma unroll
       for (int r = 0; r < RPL; ++r)
         if (roff[r] >= 0) d.U0[(((size_t)w * NCg + t) * g.M + q * RPL + r) * NP + p] = a[r];
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
       for (int r = 0; r < RPL; ++r) bu = fmaf(B[r][k], a[r], bu);
       bu = lanes_sum<LANES>(bu);
       const float vk = bu * inv;
-      if (c == 0 && live && use && (k % LANES) == q)
+      if (c == 0 && live && use && (k % LANES) == q && d.V0)
         d.V0[(((size_t)w * NCg + t) * nwin + k) * NP + p] = vk;
       if (fw_ && live && use) {
         const uint32_t pc = __ldg(posw + (size_t)k * g.P + posidx);

@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) k_qr_out(Problem pb, DeviceBuffers d, int
     }
 #pragma unroll
     for (int r = 0; r < kQR; ++r) a[r] *= inv;
-    if (c == 0 && live && use) {
+    if (c == 0 && live && use && d.U0 && d.V0) {
 #pragma unroll
       for (int r = 0; r < kQR; ++r)
         if (roff[r] >= 0) d.U0[(((size_t)w * NCg + t) * g.M + l16 * kQR + r) * NP + p] = a[r];
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
     float a[RX];  // u_t rows
 #pragma unroll
     for (int r = 0; r < RX; ++r) a[r] = (live ? __ldg(X + ct * XR + q * RX + r) : 0.f) * inv;
-    if (c == 0 && live && use) {
+    if (c == 0 && live && use && d.U0 && d.V0) {
 #pragma unroll
       for (int r = 0; r < RX; ++r)
         if (roff[r] >= 0) d.U0[(((size_t)w * NCg + t) * g.M + q * RX + r) * NP + p] = a[r];
@@ -527,7 +527,7 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
       for (int r = 0; r < RX; ++r) bu = fmaf(B[r][k], a[r], bu);
       bu = lanes_sum<4>(bu);
       const float vk = bu * inv;
-      if (c == 0 && live && use && (k % 4) == q)
+      if (c == 0 && live && use && (k % 4) == q && d.V0)
         d.V0[(((size_t)w * NCg + t) * nwin + k) * NP + p] = vk;
       if (fw_ && live && use) {
         const float4 g4 = *reinterpret_cast<const float4*>(gs + k * 4 * RX);
