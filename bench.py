@@ -10,7 +10,10 @@ value: frames/s with the sequence already resident in HBM (pgsvt_denoise_device
 on torch's current stream, CUDA events around the timed steps).
 e2e:   frames/s through pgsvt_denoise with pinned host buffers (host->device
 copy of the input and device->host copy of the result inside every step).
-cpu_baseline: the FP64 oracle port on the host cores, timed on a bounded sample.
+cpu_baseline: the FP64 oracle port on the host cores: 16 full windows of the
+              sequence, one per thread (the reference's std::thread fan-out
+              over output frames), measured, no extrapolation.  The same run
+              gives the `parity` object: the oracle's frames against the GPU's.
 
 Run with torchrun for N > 1: every rank denoises its own sequence (weak
 scaling, no collective on the data path); rank 0 prints one JSON line.
@@ -18,6 +21,7 @@ scaling, no collective on the data path); rank 0 prints one JSON line.
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -32,7 +36,6 @@ import __graft_entry__ as entry  # noqa: E402
 
 METRIC = "frames/s at PGURE-optimal lambda (512^2, 4x4, T=15)"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
-SM_COUNT = 152
 
 
 def parse():
@@ -49,23 +52,59 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-lambda arm")
     ap.add_argument("--no-default-path", action="store_true",
                     help="skip timing the reference's default path (median 5 + noise estimation)")
-    ap.add_argument("--batch", type=int, default=0,
-                    help="also time pgsvt_denoise_batch on this many uneven sequences")
+    ap.add_argument("--batch", type=int, default=64,
+                    help="also time pgsvt_denoise_batch on this many uneven sequences (0: skip)")
     ap.add_argument("--batch-full", action="store_true",
                     help="batch sequences of the full configuration (sides to 1024, 30-300 "
                          "frames) instead of the bench-time scaled ones")
     ap.add_argument("--autotune", type=int, default=1,
                     help="SVD kernel form: 1 tuned (default), 0 registers, 2 more lanes, "
                     "3 shared memory, 4 eight rows per lane")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-stride", type=int, default=0, help="patch stride of the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the oracle leg (CPU baseline and parity)")
+    ap.add_argument("--cpu-windows", type=int, default=16,
+                    help="full windows of the oracle leg (one per host thread)")
     return ap.parse_args()
 
 
+# The parameters of the benchmark workload, shared by the GPU arms and the
+# oracle: PGURESVT's arguments (pguresvt.hpp:17-38) with the lambda search of
+# the library (8 points, 4 rounds) on both sides.
+def workload_kw(bs, a, m, s):
+    return dict(traj_length=15, block_size=bs, block_overlap=1, motion_window=7,
+                median_size=-1, random_seed=7, optimize_pgure=1, alpha=a, mu=m, sigma=s)
+
+
 def params(capi, a, m, s, bs, hint, autotune=1):
-    return capi.default_params(traj_length=15, block_size=bs, block_overlap=1, motion_window=7,
-                               median_size=-1, random_seed=7, optimize_pgure=1, alpha=a, mu=m,
-                               sigma=s, lambda_hint=hint, autotune=autotune)
+    return capi.default_params(lambda_hint=hint, autotune=autotune, **workload_kw(bs, a, m, s))
+
+
+def workload_config(S, nimg, bs, a, m, s, hint=-1.0):
+    """The `config` object of both arms' lines."""
+    return {"workload": "lattice_512: %dx%dx%d f32, patch %d (m=%d), T=15, ARPS mw=7, "
+                        "PGURE on, alpha=%g mu=%g sigma=%g, median off"
+                        % (S, S, nimg, bs, bs * bs, a, m, s),
+            "lambda_search": "plain" if hint <= 0 else "hinted %g" % hint,
+            "l2": "input larger than L2 (no flush needed)"}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=20).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
 
 
 class ClockSampler:
@@ -207,55 +246,128 @@ def run_batch(capi, n, seed, slots=2, full=False):
                        "%d sequences)" % n)}
 
 
-def cpu_baseline(noisy, nm, bs, evals_per_window, stride, threads, nsample):
-    """Oracle port timed on the host cores: one window per thread, every
-    `stride`-th patch position, `evals_per_window` risk evaluations."""
+def window_of(X, t, fw):
+    """The normalised window of output frame t (pguresvt.hpp:100-120)."""
+    nt = X.shape[2]
+    s0 = 0 if t < fw else (nt - 2 * fw - 1 if t >= nt - fw else t - fw)
+    u = np.asarray(X[:, :, s0:s0 + 2 * fw + 1], np.float64)
+    return np.asfortranarray(u / u.max())
+
+
+def oracle_leg(capi, noisy, clean, nm, bs, Y, est, risk, nev, nwin, threads):
+    """CPU baseline and parity on `nwin` full windows around the middle of the
+    sequence: the oracle denoises them on `nwin` threads, one window each
+    (the reference's fan-out over output frames, utils.hpp:108-168), with the
+    same lambda search schedule as the GPU; its wall time is the baseline and
+    its frames are compared with the GPU's (Y, est: the GPU run's outputs)."""
     O = entry.load_oracle()
     a, m, s = nm
     nimg = noisy.shape[2]
-    first = max(0, nimg // 2 - nsample // 2)
+    nwin = max(1, min(nwin, nimg))
+    fb = nimg // 2 - nwin // 2
+    f = slice(fb, fb + nwin)
+    X64 = np.asfortranarray(noisy, dtype=np.float64)
     t0 = time.perf_counter()
-    sec = O.time_sample(noisy, first, nsample, threads, stride, evals_per_window,
-                        traj_length=15, block_size=bs, motion_window=7, median_size=-1,
-                        random_seed=7, optimize_pgure=1, alpha=a, mu=m, sigma=s)
+    Y0, est0, rep = O.denoise(X64, frame_begin=fb, frame_end=fb + nwin, n_jobs=nwin,
+                              **workload_kw(bs, a, m, s))
     wall = time.perf_counter() - t0
-    return {"value": threads / sec, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": "%d windows (frames %d-%d) on %d threads, every %d-th patch position, "
-                      "%d risk evaluations/window; per-window time = %d x patch-proportional "
-                      "work + per-voxel work (%.1f s wall)"
-                      % (nsample, first, first + nsample - 1, threads, stride, evals_per_window,
-                         stride, wall),
-            "seconds_per_window": sec}
-
-
-def choose_stride(side, bs):
-    # about 1-3 s of single-thread work per sampled window
-    P = (side - bs + 1) ** 2
-    return max(1, P // 4096)
+    model = cpu_model()
+    cpu = {"value": nwin / wall, "unit": "frames/s", "cores": nwin, "kind": "port",
+           "cpu_model": model, "seconds": wall,
+           "risk_evals_per_window": rep.risk_evals / max(1, rep.windows),
+           "sample": "%d full windows (output frames %d-%d of the sequence), one per thread "
+                     "(the reference's std::thread fan-out over output frames), every patch, "
+                     "the lambda search schedule of the GPU plain search; measured wall time, "
+                     "no extrapolation" % (nwin, fb, fb + nwin - 1)}
+    # parity: the denoised frames against the clean sequence, GPU and oracle
+    cl = clean[:, :, f]
+    pg, po = psnr(cl, Y[:, :, f]), psnr(cl, Y0[:, :, f])
+    par = {"frames": "%d-%d" % (fb, fb + nwin - 1), "windows": nwin,
+           "psnr_gpu_db": pg, "psnr_ref_db": po, "psnr_delta_db": pg - po,
+           "psnr_gpu_vs_ref_db": psnr(Y0[:, :, f], Y[:, :, f]),
+           "max_abs_diff_rel": float(np.abs(Y[:, :, f] - Y0[:, :, f]).max()
+                                     / np.abs(Y0[:, :, f]).max()),
+           "lambda_gpu": [float(v) for v in est[f, 0]],
+           "lambda_ref": [float(v) for v in est0[f, 0]],
+           "risk_evals_gpu": float(np.mean(nev[f])),
+           "risk_evals_ref": rep.risk_evals / max(1, rep.windows)}
+    # trajectories, singular values and the risk gap on the first and last
+    # windows of the sample (oracle stages on all host threads)
+    O.set_threads(threads)
+    try:
+        ntc, fw, nw = O.window_geometry(15, bs)
+        mv_equal, sv_max, sv_mean, sv_abs, gaps = True, 0.0, [], 0.0, []
+        for t in (fb, fb + nwin - 1):
+            u = window_of(noisy, t, fw)
+            r0, c0 = O.arps_window(u, bs, 7, t, fw, nimg)
+            r1, c1 = capi.arps_window(u, bs, 7, t, fw, nimg)
+            mv_equal = mv_equal and np.array_equal(r0, r1) and np.array_equal(c0, c1)
+            S0 = O.svd_window(u, bs, 1, r0, c0)
+            S1 = capi.svd_window(u, bs, 1, r0, c0).astype(np.float64)
+            smax = S0[:, :1]
+            big = S0 > 1e-3 * smax
+            rel = np.abs(S1 - S0) / np.maximum(S0, 1e-300)
+            sv_max = max(sv_max, float(rel[big].max()))
+            sv_mean.append(float(rel[big].mean()))
+            sv_abs = max(sv_abs, float((np.abs(S1 - S0) / smax).max()))
+            rr = O.risk_window(u, bs, 1, r0, c0, [est[t, 0], est0[t, 0]], a, m, s, 7)
+            gaps.append(float((rr[0] - rr[1]) / abs(rr[1])))
+    finally:
+        O.set_threads(1)
+    par.update({"motion_vectors_identical": bool(mv_equal), "sv_rel_err_max": sv_max,
+                "sv_rel_err_mean": float(np.mean(sv_mean)), "sv_abs_err_max_over_smax": sv_abs,
+                "sv_note": "FP32 Jacobi vs FP64 LAPACK dgesdd on windows %d and %d (every "
+                           "patch); relative errors over s > 1e-3 s_max" % (fb, fb + nwin - 1),
+                "risk_gap_max": max(gaps),
+                "risk_gap_note": "oracle risk at the GPU's lambda over its own minimum, "
+                                 "windows %d and %d" % (fb, fb + nwin - 1)})
+    return cpu, par
 
 
 def run_reference(args, rank):
-    """Reference arm: the oracle port (the reference does not build here)."""
+    """Reference arm: the FP64 oracle port on all host threads (the reference
+    itself does not build here: Armadillo and NLopt are absent).  One step is
+    one complete output frame of the benchmark sequence: its window's noise
+    estimate, ARPS, the four decompositions and the lambda search (the same
+    schedule as the GPU plain search), every patch, the window's work spread
+    over all host threads; consecutive steps take consecutive frames."""
     if rank != 0:
         return
     noisy, nm = make_workload(args.side, args.frames, args.seed)
+    a, m, s = nm
+    O = entry.load_oracle()
     threads = os.cpu_count() or 1
-    stride = args.cpu_stride or choose_stride(args.side, args.patch)
-    evals = 40
-    vals = []
+    X64 = np.asfortranarray(noisy, dtype=np.float64)
+    nimg = args.frames
+    kw = workload_kw(args.patch, a, m, s)
+    times, evals = [], []
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(noisy, nm, args.patch, evals, stride, threads, threads)
+        t = (nimg // 2 - args.warmup + i) % nimg
+        t0 = time.perf_counter()
+        _, _, rep = O.denoise(X64, frame_begin=t, frame_end=t + 1, n_jobs=1,
+                              window_threads=threads, **kw)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(r)
-    v = statistics.median([r["value"] for r in vals])
+            times.append(dt)
+            evals.append(rep.risk_evals)
+    ms = 1e3 * sum(times) / len(times)
+    v = len(times) / sum(times)
     line = {"metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.frames / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded blob+lattice sequence, Poisson-Gaussian noise)",
-            "config": {"workload": "lattice_512: %dx%dx%d f32, patch %d, T=15, ARPS mw=7, PGURE on"
-                                   % (args.side, args.side, args.frames, args.patch)},
+            "config": workload_config(args.side, nimg, args.patch, a, m, s),
             "impl": "reference",
-            "cpu_baseline": {k: vals[-1][k] for k in ("kind", "cores", "sample")} | {"value": v},
+            "cpu_baseline": {"kind": "port", "cores": threads, "cpu_model": cpu_model(),
+                             "value": v,
+                             "sample": "one complete output frame per step (frames %d-%d): "
+                                       "noise estimate, ARPS, 4 decompositions, %.1f risk "
+                                       "evaluations (the GPU plain search's schedule), every "
+                                       "patch, on %d threads inside the window; measured, no "
+                                       "extrapolation" % ((nimg // 2) % nimg,
+                                                          (nimg // 2 + args.steps - 1) % nimg,
+                                                          float(np.mean(evals)), threads)},
+            "risk_evals_per_window": float(np.mean(evals)),
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -320,9 +432,10 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * nimg / (ms / 1e3)
+    Y_plain = y.cpu().numpy().reshape(noisy.shape, order="F")
     plain = {"risk": risk.cpu().numpy().copy(), "evals": nev.cpu().numpy().copy(),
-             "lambda": est.cpu().numpy()[:nimg].copy(),
-             "psnr": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
+             "est": est.cpu().numpy().reshape(4, nimg).T.copy(),
+             "psnr": psnr(clean, Y_plain)}
 
     # ---- learned-lambda form: the shipped MLP's proposal + narrow search
     learned = None
@@ -404,16 +517,19 @@ def main():
     svd_flop = svd_flops(M, N) * st.svd_matrices / max(1, st.svd_launches)
     peaks = json.load(open(PEAKS_PATH)) if os.path.exists(PEAKS_PATH) else {}
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
     svd_kernels = {0: "k_bsweep + k_bout" if M <= 16 and N <= 15 else "k_svd",
                    4: "k_qr + k_xsweep + k_qr_out"}.get(int(st.svd_variant), "k_svd")
     roof = {"kernel": "SVD stage: %s (batched one-sided Jacobi, FP32 CUDA cores)" % svd_kernels,
             "bound": "fp32",
             "achieved": svd_flop / svd_t / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": svd_flop / svd_t / 1e12 / fp32_peak,
-            "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x 2 flop x %.0f MHz "
-                           "(sm_max_mhz of MEASURED_PEAKS.json); MEASURED_PEAKS has no "
-                           "non-tensor FP32 figure" % sm_mhz,
+            "peak_source": "nominal FP32 FMA rate: %d SMs (the device's multiprocessor "
+                           "count) x 128 lanes x 2 flop x %.0f MHz (sm_max_mhz of "
+                           "MEASURED_PEAKS.json); MEASURED_PEAKS has no non-tensor FP32 figure"
+                           % (sm_count, sm_mhz),
+            "sm_count": sm_count,
             "algorithmic_flops_per_launch": svd_flop, "avg_launch_ms": svd_t * 1e3,
             "traffic": None}
     prof = os.path.join(ROOT, "profiles", "traffic.json")
@@ -448,11 +564,7 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded blob+lattice sequence, Poisson-Gaussian noise); input "
                     "%.0f MB > L2 per step" % (noisy.nbytes / 1e6),
-            "config": {"workload": "lattice_512: %dx%dx%d f32, patch %d (m=%d), T=15, ARPS mw=7, "
-                                   "PGURE on, alpha=%g mu=%g sigma=%g, median off"
-                                   % (S, S, nimg, args.patch, M, a, m, s),
-                       "lambda_search": "plain" if args.hint <= 0 else "hinted %g" % args.hint,
-                       "l2": "input larger than L2 (no flush needed)"},
+            "config": workload_config(S, nimg, args.patch, a, m, s, args.hint),
             "e2e": e2e, "roofline": roof, "clocks": clk, "learned": learned,
             "psnr_db_vs_clean": plain["psnr"],
             "gpu_launches": int(sum(x.kernel_launches for x in stats)),
@@ -470,23 +582,25 @@ def main():
         pd = capi.default_params(traj_length=15, block_size=args.patch, motion_window=7,
                                  median_size=5, random_seed=7, autotune=args.autotune)
 
-        def timed_once(pp):
+        def timed(pp, steps):
+            """Device time per step of `steps` steps after one untimed step."""
             step(pp)
             torch.cuda.synchronize()
             g0 = torch.cuda.Event(enable_timing=True)
             g1 = torch.cuda.Event(enable_timing=True)
             g0.record(stream)
-            step(pp)
+            for _ in range(steps):
+                step(pp)
             g1.record(stream)
             torch.cuda.synchronize()
-            return g0.elapsed_time(g1)
+            return g0.elapsed_time(g1) / steps
 
-        dms = timed_once(pd)
+        dms = timed(pd, args.steps)
         dp_risk = risk.cpu().numpy().copy()
         dp_evals = float(nev.cpu().numpy().mean())
         dp_psnr = psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))
         line["default_path"] = {"value": nimg / (dms / 1e3), "unit": "frames/s",
-                                "ms_per_step": dms, "steps": 1, "psnr_db": dp_psnr,
+                                "ms_per_step": dms, "steps": args.steps, "psnr_db": dp_psnr,
                                 "risk_evals_per_window": dp_evals,
                                 "noise_estimates_frame0": [float(v) for v in
                                                            est.cpu().numpy().reshape(4, nimg)[1:, 0]],
@@ -496,21 +610,22 @@ def main():
         if not args.no_learned and args.patch == 4:  # the learned proposal on the default path
             model = pkg.learned.load_model()
             pd.lambda_model = model.ctypes.data
-            lms = timed_once(pd)
+            lms = timed(pd, args.steps)
             gap = (risk.cpu().numpy() - dp_risk) / np.abs(dp_risk)
             line["default_path"]["learned"] = {
                 "value": nimg / (lms / 1e3), "unit": "frames/s", "ms_per_step": lms,
+                "steps": args.steps, "speedup_vs_plain": dms / lms,
                 "risk_evals_per_window": float(nev.cpu().numpy().mean()),
                 "risk_gap_max": float(gap.max()), "risk_gap_mean": float(gap.mean()),
                 "windows_gap_le_1pct": float(np.mean(gap <= 0.01)),
                 "psnr_db": psnr(clean, y.cpu().numpy().reshape(noisy.shape, order="F"))}
     if args.batch:
         line["batch"] = run_batch(capi, args.batch, args.seed, full=args.batch_full)
-    if not args.no_cpu_baseline and world == 1:  # the CPU baseline: rank 0 at N = 1 only
+    if not args.no_cpu_baseline and world == 1:  # CPU baseline and parity: rank 0 at N = 1
         threads = os.cpu_count() or 1
-        line["cpu_baseline"] = cpu_baseline(noisy, (a, m, s), args.patch, evals_per_window,
-                                            args.cpu_stride or choose_stride(S, args.patch),
-                                            threads, threads)
+        line["cpu_baseline"], line["parity"] = oracle_leg(
+            capi, noisy, clean, (a, m, s), args.patch, Y_plain, plain["est"], plain["risk"],
+            plain["evals"], min(args.cpu_windows, threads), threads)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

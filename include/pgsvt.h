@@ -306,6 +306,14 @@ int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin,
                      const int32_t* rows, const int32_t* cols, float* S,
                      uint32_t* npatch);
 
+/* pgsvt_svd_window that also fills `st` (may be NULL): svd_matrices,
+ * svd_warp_sweeps and svd_fp64_tests, the Jacobi convergence decisions taken
+ * from FP64 inner products on near-degenerate singular pairs.              */
+int pgsvt_svd_window_ex(const double* u, uint32_t nrows, uint32_t nwin,
+                        uint32_t block_size, uint32_t block_overlap,
+                        const int32_t* rows, const int32_t* cols, float* S,
+                        uint32_t* npatch, pgsvt_status* st);
+
 /* Singular-value thresholding reconstruction of one window at `lambda`
  * (SVT::Reconstruct, svt.hpp:121-167): v is nrows x nrows x nwin double. */
 int pgsvt_reconstruct_window(const double* u, uint32_t nrows, uint32_t nwin,

@@ -23,7 +23,10 @@ LIB = os.path.join(BUILD, "libpgsvt_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_PROBES = os.path.join(REF_DIR, "ref_probes")
 REF_MEDIAN = os.path.join(REF_DIR, "libref_medfilter.so")
-REFERENCE_SRC = "/root/reference/src"
+# The reference tree: PGSVT_REFERENCE names its root; the default is where this
+# recipe expects the read-only checkout.
+REFERENCE_ROOT = os.environ.get("PGSVT_REFERENCE", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE_ROOT, "src")
 
 
 def _stale(target, sources):
@@ -42,7 +45,7 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread",
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-pthread",
            "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
            "-o", tmp, src, src2]
     if verbose:

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <numeric>
 #include <stdexcept>
+#include <thread>
 #include <vector>
 
 namespace orc_noise {
@@ -221,34 +222,60 @@ struct Estimator {
     return maxValue * M / dyn;
   }
 
-  // Estimate (noise.hpp:36-152) on a normalised window: Ny x Nx x T.
+  // Leaf statistics of one frame (noise.hpp:40-104), appended in the
+  // reference's order.
+  void frame_stats(const double* uf, uint32_t ny, uint32_t nx, std::vector<double>& means,
+                   std::vector<double>& vars) {
+    const Frame fr{uf, ny};
+    ti.assign(1, 0);
+    tj.assign(1, 0);
+    ts.assign(1, nx);
+    del.clear();
+    quadtree(fr, 0);
+    std::vector<uint32_t> d = del;
+    std::sort(d.begin(), d.end());
+    d.erase(std::unique(d.begin(), d.end()), d.end());
+    std::vector<char> keep(ti.size(), 1);
+    for (size_t k = d.size() > 0 ? d.size() - 1 : 0; k > 0; --k) keep[d[k]] = 0;
+    for (size_t n = 0; n < ti.size(); ++n) {
+      if (!keep[n]) continue;
+      const uint32_t x = ti[n], y = tj[n], s = ts[n];
+      std::vector<double> col((size_t)s * s);
+      for (uint32_t c = 0; c < s; ++c)
+        for (uint32_t r = 0; r < s; ++r) col[r + (size_t)c * s] = fr.at(x + r, y + c);
+      const double m = robust_mean(col);
+      const double v = robust_var(laplace(col, s));
+      if (m >= 0.0 && v >= 0.0) {  // noise.hpp:100-102 (-1 marks unused slots)
+        means.push_back(m);
+        vars.push_back(v);
+      }
+    }
+  }
+
+  // Estimate (noise.hpp:36-152) on a normalised window: Ny x Nx x T.  The
+  // frames' statistics are independent: with threads > 1 they are computed
+  // concurrently (one estimator per frame) and concatenated in frame order.
   void estimate(const double* u, uint32_t ny, uint32_t nx, uint32_t T, double& alpha,
-                double& mu, double& sigma) {
+                double& mu, double& sigma, uint32_t threads = 1) {
     std::vector<double> means, vars;
-    for (uint32_t f = 0; f < T; ++f) {
-      const Frame fr{u + (size_t)f * nx * ny, ny};
-      ti.assign(1, 0);
-      tj.assign(1, 0);
-      ts.assign(1, nx);
-      del.clear();
-      quadtree(fr, 0);
-      std::vector<uint32_t> d = del;
-      std::sort(d.begin(), d.end());
-      d.erase(std::unique(d.begin(), d.end()), d.end());
-      std::vector<char> keep(ti.size(), 1);
-      for (size_t k = d.size() > 0 ? d.size() - 1 : 0; k > 0; --k) keep[d[k]] = 0;
-      for (size_t n = 0; n < ti.size(); ++n) {
-        if (!keep[n]) continue;
-        const uint32_t x = ti[n], y = tj[n], s = ts[n];
-        std::vector<double> col((size_t)s * s);
-        for (uint32_t c = 0; c < s; ++c)
-          for (uint32_t r = 0; r < s; ++r) col[r + (size_t)c * s] = fr.at(x + r, y + c);
-        const double m = robust_mean(col);
-        const double v = robust_var(laplace(col, s));
-        if (m >= 0.0 && v >= 0.0) {  // noise.hpp:100-102 (-1 marks unused slots)
-          means.push_back(m);
-          vars.push_back(v);
-        }
+    if (threads <= 1) {
+      for (uint32_t f = 0; f < T; ++f) frame_stats(u + (size_t)f * nx * ny, ny, nx, means, vars);
+    } else {
+      std::vector<std::vector<double>> fm(T), fv(T);
+      std::vector<std::thread> th;
+      const uint32_t nt = std::min(threads, T);
+      for (uint32_t k = 0; k < nt; ++k)
+        th.emplace_back([&, k] {
+          for (uint32_t f = T * k / nt; f < T * (k + 1) / nt; ++f) {
+            Estimator e;
+            e.method = method;
+            e.frame_stats(u + (size_t)f * nx * ny, ny, nx, fm[f], fv[f]);
+          }
+        });
+      for (auto& t : th) t.join();
+      for (uint32_t f = 0; f < T; ++f) {
+        means.insert(means.end(), fm[f].begin(), fm[f].end());
+        vars.insert(vars.end(), fv[f].begin(), fv[f].end());
       }
     }
     std::vector<size_t> idx(means.size());
@@ -297,8 +324,9 @@ struct Estimator {
 
 // C++ entry used by pgsvt_oracle.cpp and the C API
 void orc_noise_estimate_impl(const double* u, uint32_t ny, uint32_t nx, uint32_t T,
-                             uint32_t method, double& alpha, double& mu, double& sigma) {
+                             uint32_t method, double& alpha, double& mu, double& sigma,
+                             uint32_t threads) {
   orc_noise::Estimator e;
   e.method = method;
-  e.estimate(u, ny, nx, T, alpha, mu, sigma);
+  e.estimate(u, ny, nx, T, alpha, mu, sigma, threads);
 }

@@ -43,6 +43,7 @@ class OrcParams(ctypes.Structure):
         ("hint_flat", ctypes.c_double), ("autotune", ctypes.c_uint32),
         ("lambda_hints", ctypes.c_void_p),
         ("risk_out", ctypes.c_void_p), ("evals_out", ctypes.c_void_p),
+        ("window_threads", ctypes.c_uint32),
     ]
 
 
@@ -58,7 +59,8 @@ DEFAULTS = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7,
                 compat_flags=COMPAT_ALL, search_points=8, search_rounds=4,
                 window_batch=0, lambda_hint=-1.0, hint_span=2.0, frame_begin=0,
                 frame_end=0, lambda_model=None, hint_points=4, hint_rounds=1, hint_flat=1e-3,
-                autotune=0, lambda_hints=None, risk_out=None, evals_out=None)
+                autotune=0, lambda_hints=None, risk_out=None, evals_out=None,
+                window_threads=1)
 
 _lib = None
 
@@ -102,9 +104,7 @@ def lib():
         L.orc_median_filter.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3
         L.orc_denoise.argtypes = [ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [
             P(OrcParams), ctypes.c_void_p, ctypes.c_void_p, P(OrcReport)]
-        L.orc_time_sample.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
-                                      P(OrcParams)] + [ctypes.c_uint32] * 5 + [
-                                          P(ctypes.c_double)]
+        L.orc_set_threads.argtypes = [ctypes.c_uint32]
         L.orc_set_dgesdd(_dgesdd_pointer())
         _lib = L
     return _lib
@@ -130,6 +130,12 @@ def make_params(**kw):
     for k, v in d.items():
         setattr(p, k, v)
     return p
+
+
+def set_threads(n):
+    """Threads inside one window for the per-stage functions below (arps_window,
+    svd_window, reconstruct_window, risk_window); results do not depend on it."""
+    lib().orc_set_threads(max(1, int(n)))
 
 
 def window_geometry(traj_length, block_size):
@@ -257,14 +263,3 @@ def denoise(X, lambda_hints=None, **kw):
     out = types.SimpleNamespace(windows=rep.windows, risk_evals=rep.risk_evals,
                                 seconds=rep.seconds, risk=risk, evals=evals)
     return Y, est, out
-
-
-def time_sample(X, first, nwindows, threads, stride, evals, **kw):
-    """Mean single-thread seconds per window of a thinned timing sample."""
-    X = _cube(X)
-    nr, _, nt = X.shape
-    p = make_params(**kw)
-    sec = ctypes.c_double()
-    _check(lib().orc_time_sample(_ptr(X), nr, nt, ctypes.byref(p), first, nwindows, threads,
-                                 stride, evals, ctypes.byref(sec)))
-    return sec.value

@@ -28,7 +28,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <limits>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -37,20 +39,40 @@
 
 // noise_oracle.cpp: NoiseEstimator::Estimate (noise.hpp:36-152)
 void orc_noise_estimate_impl(const double* u, uint32_t ny, uint32_t nx, uint32_t T,
-                             uint32_t method, double& alpha, double& mu, double& sigma);
+                             uint32_t method, double& alpha, double& mu, double& sigma,
+                             uint32_t threads = 1);
 
 namespace {
 
 thread_local std::string g_err;
 orc_dgesdd_fn g_dgesdd = nullptr;
+uint32_t g_stage_threads = 1;  // threads of the per-stage entry points (orc_set_threads)
 
-// Per-thread stage clocks for the timing sample: seconds spent in work that
-// scales with the number of patches vs work over every voxel of the window.
-thread_local bool tl_timing = false;
-thread_local double tl_patch_s = 0.0, tl_voxel_s = 0.0;
-using Clock = std::chrono::steady_clock;
-inline double since(Clock::time_point a) {
-  return std::chrono::duration<double>(Clock::now() - a).count();
+// fn(begin, end, tid) over [0, n) in `threads` contiguous chunks, one
+// std::thread each (on the calling thread when threads <= 1).  Used inside one
+// window: every chunk writes its own outputs, so results do not depend on the
+// thread count.
+template <typename Fn>
+void par_chunks(size_t n, uint32_t threads, Fn&& fn) {
+  if (threads <= 1 || n < 2) {
+    fn((size_t)0, n, 0u);
+    return;
+  }
+  const uint32_t nt = (uint32_t)std::min<size_t>(threads, n);
+  std::vector<std::thread> th;
+  std::vector<std::exception_ptr> ex(nt);
+  th.reserve(nt);
+  for (uint32_t k = 0; k < nt; ++k)
+    th.emplace_back([&, k] {
+      try {
+        fn(n * k / nt, n * (k + 1) / nt, k);
+      } catch (...) {
+        ex[k] = std::current_exception();
+      }
+    });
+  for (auto& t : th) t.join();
+  for (auto& e : ex)
+    if (e) std::rethrow_exception(e);
 }
 
 constexpr uint32_t kCompatSwap = 0x1u;        // pguresvt.hpp:133 vs pgure.hpp:26-30
@@ -170,7 +192,7 @@ struct Arps {
   std::vector<int32_t> mrow, mcol;  // motions(2, P, 2*fw)
   int32_t* prow;
   int32_t* pcol;                    // patches(2, P, nwin)
-  uint32_t stride = 1;              // timing samples only
+  uint32_t threads = 1;             // threads over the positions of a frame pair
 
   Arps(const double* a, Geom gg, uint32_t m, int32_t* r, int32_t* c)
       : A(a), g(gg), mw(m), oo(1.0 / (gg.bs * gg.bs)), prow(r), pcol(c) {
@@ -207,8 +229,9 @@ struct Arps {
     const int W = 2 * (int)mw + 1, M = (int)mw, bs = (int)g.bs, S = (int)g.S;
     const int P = (int)g.P, n1 = 1 + (int)g.nMbs;
     static const int SD[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};  // (dx, dy)
+    par_chunks((size_t)P, threads, [&](size_t b, size_t e, uint32_t) {
     std::vector<uint8_t> seen((size_t)W * W);
-    for (int it = 0; it < P; it += (int)stride) {
+    for (int it = (int)b; it < (int)e; ++it) {
       double c[6];
       for (double& x : c) x = kCostSentinel;
       std::fill(seen.begin(), seen.end(), 0);
@@ -278,6 +301,7 @@ struct Arps {
       prow[(size_t)a2 * P + it] = y;
       pcol[(size_t)a2 * P + it] = x;
     }
+    });
   }
 
   // MotionEstimator::Estimate (arps.hpp:52-134).
@@ -329,9 +353,12 @@ struct Svt {
   const int32_t* prow;
   const int32_t* pcol;
   uint32_t m, n;
-  std::vector<double> U, S, VT;  // per patch: m*n, n, n*n
+  // per patch: m*n, n, n*n; left uninitialised until dgesdd writes every
+  // entry (the threads that compute a patch also first touch its pages)
+  std::unique_ptr<double[]> U, S, VT;
   bool expw;
   std::vector<double> weights;   // coverage count per voxel (lambda independent)
+  uint32_t threads = 1;          // threads inside this window
 
   Svt(Geom gg, std::vector<int64_t> pl, const int32_t* r, const int32_t* c, bool e)
       : g(gg), plist(std::move(pl)), prow(r), pcol(c), m(gg.bs * gg.bs), n(gg.nwin), expw(e) {}
@@ -349,39 +376,46 @@ struct Svt {
     }
   }
 
-  // Decompose (svt.hpp:58-118)
+  // Decompose (svt.hpp:58-118); patches split over `threads`, each with its
+  // own LAPACK workspace, writing its own factors.
   void decompose(const double* u) {
     if (!g_dgesdd) throw Fail(2, "oracle: no LAPACK dgesdd bound (orc_set_dgesdd)");
     const size_t N = np();
-    U.assign(N * m * n, 0.0);
-    S.assign(N * n, 0.0);
-    VT.assign(N * n * n, 0.0);
-    std::vector<double> blk((size_t)m * n), work(1);
-    std::vector<int> iwork(8 * n);
-    int M = (int)m, Nn = (int)n, lda = M, ldu = M, ldvt = Nn, lwork = -1, info = 0;
-    char jobz = 'S';
-    g_dgesdd(&jobz, &M, &Nn, blk.data(), &lda, S.data(), U.data(), &ldu, VT.data(),
-             &ldvt, work.data(), &lwork, iwork.data(), &info);
-    lwork = std::max(1, (int)work[0]);
-    work.resize(lwork);
-    auto c0 = Clock::now();
-    for (size_t it = 0; it < N; ++it) {
-      gather(u, it, blk.data());
-      g_dgesdd(&jobz, &M, &Nn, blk.data(), &lda, &S[it * n], &U[it * m * n], &ldu,
-               &VT[it * n * n], &ldvt, work.data(), &lwork, iwork.data(), &info);
-      if (info != 0) throw Fail(3, "oracle: dgesdd failed, info=" + std::to_string(info));
+    U.reset(new double[N * m * n]);
+    S.reset(new double[N * n]);
+    VT.reset(new double[N * n * n]);
+    int lwork;
+    {
+      std::vector<double> blk((size_t)m * n), work(1), s1(n), u1((size_t)m * n), v1((size_t)n * n);
+      std::vector<int> iwork(8 * n);
+      int M = (int)m, Nn = (int)n, lda = M, ldu = M, ldvt = Nn, lq = -1, info = 0;
+      char jobz = 'S';
+      g_dgesdd(&jobz, &M, &Nn, blk.data(), &lda, s1.data(), u1.data(), &ldu, v1.data(),
+               &ldvt, work.data(), &lq, iwork.data(), &info);
+      lwork = std::max(1, (int)work[0]);
     }
-    if (tl_timing) { tl_patch_s += since(c0); c0 = Clock::now(); }
+    par_chunks(N, threads, [&](size_t b, size_t e, uint32_t) {
+      std::vector<double> blk((size_t)m * n), work(lwork);
+      std::vector<int> iwork(8 * n);
+      int M = (int)m, Nn = (int)n, lda = M, ldu = M, ldvt = Nn, lw = lwork, info = 0;
+      char jobz = 'S';
+      for (size_t it = b; it < e; ++it) {
+        gather(u, it, blk.data());
+        g_dgesdd(&jobz, &M, &Nn, blk.data(), &lda, &S[it * n], &U[it * m * n], &ldu,
+                 &VT[it * n * n], &ldvt, work.data(), &lw, iwork.data(), &info);
+        if (info != 0) throw Fail(3, "oracle: dgesdd failed, info=" + std::to_string(info));
+      }
+    });
     weights.assign(g.cube(), 0.0);
-    if (tl_timing) { tl_voxel_s += since(c0); c0 = Clock::now(); }
-    for (size_t it = 0; it < N; ++it) scatter_ones(it);
-    if (tl_timing) tl_patch_s += since(c0);
+    par_chunks(n, threads, [&](size_t kb, size_t ke, uint32_t) {  // frames split
+      for (size_t it = 0; it < N; ++it) scatter_ones(it, (uint32_t)kb, (uint32_t)ke);
+    });
   }
 
-  void scatter_ones(size_t it) {
+  void scatter_ones(size_t it, uint32_t kb, uint32_t ke) {
     const size_t P = g.P, S = g.S, F = g.frame();
     const int64_t p = plist[it];
-    for (uint32_t k = 0; k < n; ++k) {
+    for (uint32_t k = kb; k < ke; ++k) {
       const int y = prow[(size_t)k * P + p], x = pcol[(size_t)k * P + p];
       for (uint32_t c = 0; c < g.bs; ++c)
         for (uint32_t r = 0; r < g.bs; ++r) weights[(size_t)k * F + (y + r) + (x + c) * S] += 1.0;
@@ -409,37 +443,55 @@ struct Svt {
   }
 
   // Reconstruct (svt.hpp:121-167): v = average of U*diag(S')*V^T blocks.
-  void reconstruct(double lambda, double* v, uint32_t stride = 1) const {
+  // With several threads the shrunk values are computed per patch chunk and
+  // the frame columns are split in bands, each thread adding, patch by patch
+  // in order, the block entries that fall in its band: every voxel sees the
+  // same additions in the same order as with one thread.
+  void reconstruct(double lambda, double* v) const {
     const size_t P = g.P, S = g.S, F = g.frame(), N = np();
-    auto c0 = Clock::now();
     std::fill(v, v + g.cube(), 0.0);
-    if (tl_timing) { tl_voxel_s += since(c0); c0 = Clock::now(); }
-    std::vector<double> sp(n), blk((size_t)m * n);
-    for (size_t it = 0; it < N; it += stride) {
-      shrink(it, lambda, sp.data());
-      const double* u = &U[it * m * n];
-      const double* vt = &VT[it * n * n];
-      for (uint32_t k = 0; k < n; ++k)
-        for (uint32_t e = 0; e < m; ++e) {
-          double acc = 0.0;
-          for (uint32_t i = 0; i < n; ++i) acc += (u[e + (size_t)i * m] * sp[i]) * vt[i + (size_t)k * n];
-          blk[(size_t)k * m + e] = acc;
+    std::vector<double> sp(N * n);
+    par_chunks(N, threads, [&](size_t b, size_t e, uint32_t) {
+      for (size_t it = b; it < e; ++it) shrink(it, lambda, &sp[it * n]);
+    });
+    par_chunks(S, threads, [&](size_t x0, size_t x1, uint32_t) {
+      const int bs = (int)g.bs;
+      std::vector<double> us((size_t)m * n), acc(m);
+      for (size_t it = 0; it < N; ++it) {
+        const double* u = &U[it * m * n];
+        const double* vt = &VT[it * n * n];
+        const double* s = &sp[it * n];
+        const int64_t p = plist[it];
+        bool have_us = false;
+        for (size_t k = 0; k < n; ++k) {
+          const int y = prow[k * P + p], x = pcol[k * P + p];
+          if (x + bs <= (int)x0 || x >= (int)x1) continue;
+          if (!have_us) {  // u_ei * s'_i, the first product of every term
+            for (uint32_t i = 0; i < n; ++i)
+              for (uint32_t e = 0; e < m; ++e) us[e + (size_t)i * m] = u[e + (size_t)i * m] * s[i];
+            have_us = true;
+          }
+          const int cb = std::max(0, (int)x0 - x), ce = std::min(bs, (int)x1 - x);
+          const size_t e0 = (size_t)cb * bs, e1 = (size_t)ce * bs;
+          // block(e, k) = sum_i (u_ei s'_i) vt_ik, i in order: one chain per row
+          for (size_t e = e0; e < e1; ++e) acc[e] = 0.0;
+          for (uint32_t i = 0; i < n; ++i) {
+            const double w = vt[i + k * n];
+            const double* ui = &us[(size_t)i * m];
+            for (size_t e = e0; e < e1; ++e) acc[e] += ui[e] * w;
+          }
+          for (int c = cb; c < ce; ++c)
+            for (int r = 0; r < bs; ++r) v[k * F + (y + r) + (x + c) * S] += acc[r + (size_t)c * bs];
         }
-      const int64_t p = plist[it];
-      for (uint32_t k = 0; k < n; ++k) {
-        const int y = prow[(size_t)k * P + p], x = pcol[(size_t)k * P + p];
-        for (uint32_t c = 0; c < g.bs; ++c)
-          for (uint32_t r = 0; r < g.bs; ++r)
-            v[(size_t)k * F + (y + r) + (x + c) * S] += blk[(size_t)k * m + r + c * g.bs];
       }
-    }
-    if (tl_timing) { tl_patch_s += since(c0); c0 = Clock::now(); }
+    });
     const size_t C = g.cube();
-    for (size_t i = 0; i < C; ++i) {
-      const double q = v[i] / weights[i];
-      v[i] = std::isfinite(q) ? q : 0.0;
-    }
-    if (tl_timing) tl_voxel_s += since(c0);
+    par_chunks(C, threads, [&](size_t b, size_t e, uint32_t) {
+      for (size_t i = b; i < e; ++i) {
+        const double q = v[i] / weights[i];
+        v[i] = std::isfinite(q) ? q : 0.0;
+      }
+    });
   }
 };
 
@@ -461,7 +513,7 @@ struct Pgure {
 
   Pgure(Geom gg, const double* u, const std::vector<int64_t>& pl, const int32_t* r,
         const int32_t* c, double a_c, double mu_c, double sigma_c, int64_t seed,
-        bool expw, bool opt, uint32_t compat, uint32_t stride = 1)
+        bool expw, bool opt, uint32_t compat, uint32_t threads = 1)
       : g(gg), U(u), optimize(opt), intDelta1(compat & kCompatIntDelta1),
         svt0(gg, pl, r, c, expw), svt1(gg, pl, r, c, expw), svt2p(gg, pl, r, c, expw),
         svt2m(gg, pl, r, c, expw) {
@@ -475,7 +527,7 @@ struct Pgure {
       sigma = sigma_c;
     }
     sigmasq = sigma * sigma;
-    if (stride > 1) thin(stride);
+    for (Svt* s : {&svt0, &svt1, &svt2p, &svt2m}) s->threads = threads;
     svt0.decompose(U);
     if (!optimize) return;
     const size_t C = g.cube();
@@ -505,14 +557,6 @@ struct Pgure {
     R2m.resize(C);
   }
 
-  void thin(uint32_t stride) {
-    for (Svt* s : {&svt0, &svt1, &svt2p, &svt2m}) {
-      std::vector<int64_t> k;
-      for (size_t i = 0; i < s->plist.size(); i += stride) k.push_back(s->plist[i]);
-      s->plist.swap(k);
-    }
-  }
-
   // CalculatePGURE (pgure.hpp:120-137)
   double risk(double lambda) {
     ++evals;
@@ -521,7 +565,6 @@ struct Pgure {
     else svt1.reconstruct(lambda, R1.data());
     svt2p.reconstruct(lambda, R2p.data());
     svt2m.reconstruct(lambda, R2m.data());
-    const auto c0 = Clock::now();
     const size_t C = g.cube();
     const double OoN = 1.0 / (g.S * g.S * g.nwin);
     const double* u = U;
@@ -532,7 +575,6 @@ struct Pgure {
     });
     const double t4 = accu2(C, [&](size_t i) { return d2[i] * ((R2p[i] - 2 * Uhat[i]) + R2m[i]); });
     const double t5 = accu2(C, [&](size_t i) { return Uhat[i]; });
-    if (tl_timing) tl_voxel_s += since(c0);
     return OoN * (t1 - (alpha + mu) * t2 + (2 / eps1 * t3) -
                   (2 * sigmasq * alpha / (eps2 * eps2) * t4) + (2 * mu * t5) + mu) -
            sigmasq;
@@ -705,14 +747,17 @@ WindowOut run_window(const double* X, const double* Z, const orc_params& p, cons
   double na = p.alpha >= 0 ? p.alpha : -1.0, nm = p.mu >= 0 ? p.mu : -1.0;
   double ns = p.sigma >= 0 ? p.sigma : -1.0;
   if (p.optimize_pgure)
-    orc_noise_estimate_impl(u.data(), g.S, g.S, g.nwin, p.noise_method, na, nm, ns);
+    orc_noise_estimate_impl(u.data(), g.S, g.S, g.nwin, p.noise_method, na, nm, ns,
+                            std::max(1u, p.window_threads));
   std::vector<int32_t> rows((size_t)g.P * g.nwin), cols((size_t)g.P * g.nwin);
   {
     Arps a(Z ? w.data() : u.data(), g, pl.mw, rows.data(), cols.data());
+    a.threads = std::max(1u, p.window_threads);
     a.estimate(t, pl.fw, pl.nimg, p.motion_estimation != 0, p.compat_flags & kCompatZeroMotion);
   }
   Pgure pg(g, u.data(), patch_list(g.S, g.bs, pl.ov), rows.data(), cols.data(), na, nm, ns,
-           p.random_seed, p.exp_weighting != 0, p.optimize_pgure != 0, p.compat_flags);
+           p.random_seed, p.exp_weighting != 0, p.optimize_pgure != 0, p.compat_flags,
+           std::max(1u, p.window_threads));
   WindowOut out{p.lambda, 0.0, 0, na, nm, ns};
   if (p.optimize_pgure) {
     const double OoN = 1.0 / (pl.nrows * pl.nrows * pl.Ntc);  // pguresvt.hpp:60
@@ -803,6 +848,7 @@ int guarded(Fn&& fn) {
 extern "C" {
 
 void orc_set_dgesdd(orc_dgesdd_fn fn) { g_dgesdd = fn; }
+void orc_set_threads(uint32_t n) { g_stage_threads = n < 1 ? 1 : n; }
 const char* orc_last_error(void) { return g_err.c_str(); }
 
 int orc_probes(int64_t seed, uint64_t n, int8_t* d1, double* d2) {
@@ -824,6 +870,7 @@ int orc_arps_window(const double* w, uint32_t side, uint32_t nwin, uint32_t bs, 
   return guarded([&] {
     if (nwin != 2 * frame_window + 1) throw Fail(1, "nwin must be 2*frame_window+1");
     Arps a(w, Geom(side, bs, nwin), mw, rows, cols);
+    a.threads = g_stage_threads;
     a.estimate(time_iter, frame_window, nimages, motion != 0, compat & kCompatZeroMotion);
   });
 }
@@ -832,9 +879,10 @@ int orc_svd_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs, u
                    const int32_t* rows, const int32_t* cols, double* S, uint64_t* npatch) {
   return guarded([&] {
     Svt s(Geom(side, bs, nwin), patch_list(side, bs, ov), rows, cols, true);
+    s.threads = g_stage_threads;
     s.decompose(u);
     *npatch = s.np();
-    if (S) std::copy(s.S.begin(), s.S.end(), S);
+    if (S) std::copy(s.S.get(), s.S.get() + s.np() * s.n, S);
   });
 }
 
@@ -843,6 +891,7 @@ int orc_reconstruct_window(const double* u, uint32_t side, uint32_t nwin, uint32
                            double lambda, double* v) {
   return guarded([&] {
     Svt s(Geom(side, bs, nwin), patch_list(side, bs, ov), rows, cols, expw != 0);
+    s.threads = g_stage_threads;
     s.decompose(u);
     s.reconstruct(lambda, v);
   });
@@ -855,7 +904,7 @@ int orc_risk_window(const double* u, uint32_t side, uint32_t nwin, uint32_t bs, 
   return guarded([&] {
     const Geom g(side, bs, nwin);
     Pgure pg(g, u, patch_list(side, bs, ov), rows, cols, alpha, mu, sigma, seed, expw != 0,
-             true, compat);
+             true, compat, g_stage_threads);
     for (uint32_t i = 0; i < nl; ++i) risk[i] = pg.risk(lambdas[i]);
   });
 }
@@ -962,53 +1011,6 @@ int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols, uint32_t nimage
       for (uint32_t e : evals) rep->risk_evals += e;
       rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
-  });
-}
-
-int orc_time_sample(const double* X, uint32_t nrows, uint32_t nimages, const orc_params* p,
-                    uint32_t first, uint32_t nwindows, uint32_t threads, uint32_t stride,
-                    uint32_t evals, double* seconds) {
-  return guarded([&] {
-    validate(*p, nrows, nrows, nimages);
-    const Plan pl(*p, nrows, nimages);
-    const Geom g(nrows, pl.bs, pl.nwin);
-    if (first + nwindows > nimages) throw Fail(1, "sample windows out of range");
-    if (stride < 1) stride = 1;
-    // Per-window time = stride * (per-patch work) + per-voxel work, each
-    // measured on the thread that ran the window (one window per thread, as
-    // the reference's std::thread fan-out does).
-    std::vector<double> tw(nwindows, 0.0);
-    fan_out(nwindows, threads, [&](uint32_t k) {
-      const uint32_t t = first + k;
-      const size_t F = g.frame(), C = g.cube();
-      tl_timing = true;
-      tl_patch_s = tl_voxel_s = 0.0;
-      auto a0 = Clock::now();
-      std::vector<double> u(X + (size_t)pl.start(t) * F, X + (size_t)pl.start(t) * F + C);
-      double umax = u[0];
-      for (double x : u) umax = std::max(umax, x);
-      for (double& x : u) x /= umax;
-      std::vector<int32_t> rows((size_t)g.P * g.nwin), cols((size_t)g.P * g.nwin);
-      const double setup = since(a0);
-      auto a1 = Clock::now();
-      {
-        Arps a(u.data(), g, pl.mw, rows.data(), cols.data());
-        a.stride = stride;
-        a.estimate(t, pl.fw, pl.nimg, p->motion_estimation != 0,
-                   p->compat_flags & kCompatZeroMotion);
-      }
-      const double arps = since(a1);
-      Pgure pg(g, u.data(), patch_list(g.S, g.bs, pl.ov), rows.data(), cols.data(), p->alpha,
-               p->mu, p->sigma, p->random_seed, p->exp_weighting != 0, p->optimize_pgure != 0,
-               p->compat_flags, stride);
-      for (uint32_t e = 0; e < evals && p->optimize_pgure; ++e)
-        pg.risk(0.01 * std::pow(1e4, (double)e / std::max<uint32_t>(1, evals - 1)));
-      tl_timing = false;
-      tw[k] = setup + stride * (arps + tl_patch_s) + tl_voxel_s;
-    });
-    double s = 0;
-    for (double x : tw) s += x;
-    *seconds = s / nwindows;  // mean single-thread seconds per window
   });
 }
 

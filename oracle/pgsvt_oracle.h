@@ -42,6 +42,9 @@ typedef struct {
   const double* lambda_hints;
   double* risk_out;
   uint32_t* evals_out;
+  /* oracle only: threads inside each window (ARPS positions, SVD patches,
+   * reconstruction frames); results do not depend on it.  0 or 1: one. */
+  uint32_t window_threads;
 } orc_params;
 
 typedef struct {
@@ -51,6 +54,11 @@ typedef struct {
 } orc_report;
 
 void orc_set_dgesdd(orc_dgesdd_fn fn);
+
+/* Threads used inside one window by orc_arps_window, orc_svd_window,
+ * orc_reconstruct_window and orc_risk_window (default 1; results do not
+ * depend on it). */
+void orc_set_threads(uint32_t n);
 
 /* PGURE probes (pgure.hpp:167-186): delta1 (+-1) then delta2, n each. */
 int orc_probes(int64_t seed, uint64_t n, int8_t* d1, double* d2);
@@ -99,16 +107,6 @@ int orc_median_filter(const uint16_t* src, uint16_t* dst, uint32_t nx, uint32_t 
 int orc_denoise(const double* X, uint32_t nrows, uint32_t ncols,
                 uint32_t nimages, const orc_params* p, double* Y,
                 double* estimates, orc_report* rep);
-
-/* Timing sample for the CPU baseline: runs the per-window pipeline of
- * `nwindows` windows (starting at window `first`) on `threads` threads with
- * only every `stride`-th patch position kept in ARPS / SVD / reconstruction
- * and a fixed number of risk evaluations per window (`evals`).  Returns the
- * wall seconds in *seconds. */
-int orc_time_sample(const double* X, uint32_t nrows, uint32_t nimages,
-                    const orc_params* p, uint32_t first, uint32_t nwindows,
-                    uint32_t threads, uint32_t stride, uint32_t evals,
-                    double* seconds);
 
 const char* orc_last_error(void);
 

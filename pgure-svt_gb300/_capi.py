@@ -29,7 +29,8 @@ EXPORTS = ("pgsvt_default_params", "pgsvt_denoise", "pgsvt_denoise_device",
            "pgsvt_denoise_ex", "pgsvt_denoise_device_ex", "pgsvt_lambda_predict",
            "pgsvt_lambda_grad", "pgsvt_lambda_train", "pgsvt_denoise_batch",
            "pgsvt_median_filter", "pgsvt_hot_pixel_filter",
-           "pgsvt_arps_window", "pgsvt_svd_window", "pgsvt_reconstruct_window",
+           "pgsvt_arps_window", "pgsvt_svd_window", "pgsvt_svd_window_ex",
+           "pgsvt_reconstruct_window",
            "pgsvt_risk_window", "pgsvt_svd_window_noalloc", "pgsvt_last_error",
            "pgsvt_version")
 LAMBDA_FEATURES = 67
@@ -137,6 +138,7 @@ def load(path=LIB_PATH):
     L.pgsvt_lambda_train.argtypes = [vp, vp, vp, u32, P(TrainParams), vp, P(Status)]
     L.pgsvt_arps_window.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, i32, u32, vp, vp]
     L.pgsvt_svd_window.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, P(u32)]
+    L.pgsvt_svd_window_ex.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, P(u32), P(Status)]
     L.pgsvt_reconstruct_window.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp, dbl, vp]
     L.pgsvt_risk_window.argtypes = [vp, u32, u32, u32, u32, i32, vp, vp, dbl, dbl, dbl, i64,
                                     u32, vp, u32, vp]
@@ -359,8 +361,9 @@ def arps_window(w, bs, mw, time_iter, frame_window, nimages, motion=True, compat
     return rows, cols
 
 
-def svd_window(u, bs, ov, rows, cols):
-    """Singular values (npatch, nwin), descending per patch (svt.hpp:58-118)."""
+def svd_window(u, bs, ov, rows, cols, status=False):
+    """Singular values (npatch, nwin), descending per patch (svt.hpp:58-118);
+    with status=True also the call's Status (SVD sweep and FP64 counters)."""
     u, side, nwin = _window(u)
     rows = np.ascontiguousarray(rows, np.int32)
     cols = np.ascontiguousarray(cols, np.int32)
@@ -368,9 +371,10 @@ def svd_window(u, bs, ov, rows, cols):
     _check(load().pgsvt_svd_window(_ptr(u), side, nwin, bs, ov, _ptr(rows), _ptr(cols), None,
                                    ctypes.byref(n)))
     S = np.zeros((n.value, nwin), np.float32)
-    _check(load().pgsvt_svd_window(_ptr(u), side, nwin, bs, ov, _ptr(rows), _ptr(cols), _ptr(S),
-                                   ctypes.byref(n)))
-    return S
+    st = Status()
+    _check(load().pgsvt_svd_window_ex(_ptr(u), side, nwin, bs, ov, _ptr(rows), _ptr(cols),
+                                      _ptr(S), ctypes.byref(n), ctypes.byref(st)))
+    return (S, st) if status else S
 
 
 def reconstruct_window(u, bs, ov, rows, cols, lam, expw=True):

@@ -1477,10 +1477,10 @@ int pgsvt_arps_window(const double* w, uint32_t nrows, uint32_t nwin, uint32_t b
   });
 }
 
-int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
-                     uint32_t block_overlap, const int32_t* rows, const int32_t* cols, float* S,
-                     uint32_t* npatch) {
-  return guarded(nullptr, [&](Stats&) {
+int pgsvt_svd_window_ex(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                        uint32_t block_overlap, const int32_t* rows, const int32_t* cols,
+                        float* S, uint32_t* npatch, pgsvt_status* st) {
+  return guarded(st, [&](Stats& stats) {
     if (!u || !rows || !cols || !npatch) throw Fail(PGSVT_ERR_INVALID_ARG, "null pointer");
     pgsvt_params p;
     pgsvt_default_params(&p);
@@ -1494,6 +1494,14 @@ int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t bl
     ow.alloc_factors(1);
     PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
     *npatch = (uint32_t)g.NP;
+    unsigned long long c[4];
+    PGSVT_CK(cudaMemcpyAsync(c, ow.d.counters, sizeof(c), cudaMemcpyDeviceToHost, ow.s));
+    PGSVT_CK(cudaStreamSynchronize(ow.s));
+    stats.svd_launches = 1;
+    stats.svd_matrices = (uint64_t)g.NP;
+    stats.svd_sweeps = c[1];
+    stats.svd_fp64 = c[2];
+    stats.svd_variant = ow.pb.svd_variant;
     if (S) {
       std::vector<float> h((size_t)g.NC * g.NP);
       PGSVT_CK(cudaMemcpyAsync(h.data(), ow.d.sv, h.size() * 4, cudaMemcpyDeviceToHost, ow.s));
@@ -1507,6 +1515,13 @@ int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t bl
       }
     }
   });
+}
+
+int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,
+                     uint32_t block_overlap, const int32_t* rows, const int32_t* cols, float* S,
+                     uint32_t* npatch) {
+  return pgsvt_svd_window_ex(u, nrows, nwin, block_size, block_overlap, rows, cols, S, npatch,
+                             nullptr);
 }
 
 int pgsvt_reconstruct_window(const double* u, uint32_t nrows, uint32_t nwin, uint32_t block_size,

@@ -1,3 +1,4 @@
+import importlib.util
 import os
 import sys
 
@@ -9,7 +10,18 @@ if ROOT not in sys.path:
 
 import __graft_entry__ as entry  # noqa: E402
 
-REFERENCE = "/root/reference"
+
+def _reference_root():
+    """The reference tree's root, as the oracle's build recipe locates it
+    (PGSVT_REFERENCE, else the recipe's default)."""
+    spec = importlib.util.spec_from_file_location(
+        "_oracle_build_paths", os.path.join(ROOT, "oracle", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.REFERENCE_ROOT
+
+
+REFERENCE = _reference_root()
 
 
 def pytest_configure(config):

@@ -329,3 +329,92 @@ def test_large_patches_match_oracle(capi, oracle, pkg, bs, T, ov):
     err = np.abs(Y[:, :, f] - Y0[:, :, f]).max() / np.abs(Y0[:, :, f]).max()
     print("max relative difference", err)
     assert err < 1e-4
+
+
+# ---- FP64 decisions of the Jacobi convergence test
+
+def _near_degenerate_window(seed, G=8, bs=4, nwin=15):
+    """A window whose kept patches' Casorati matrices are designed: G x G
+    disjoint bs x bs blocks, block b holding B_b = U diag(s) V^T (random
+    orthonormal U, V) with three pairs of singular values equal to within
+    1e-6..1e-4 relative, and a trajectory table sending every position to a
+    block.  Returns (u, rows, cols)."""
+    rng = np.random.default_rng(seed)
+    m, S = bs * bs, bs * G
+    u = np.zeros((S, S, nwin))
+    for b in range(G * G):
+        Uq, _ = np.linalg.qr(rng.standard_normal((m, nwin)))
+        Vq, _ = np.linalg.qr(rng.standard_normal((nwin, nwin)))
+        s = np.sort(rng.uniform(0.05, 1.0, nwin))[::-1]
+        for i in (0, 4, 9):
+            s[i + 1] = s[i] * (1.0 - rng.uniform(1e-6, 1e-4))
+        B = Uq @ np.diag(s) @ Vq.T
+        r0, c0 = bs * (b % G), bs * (b // G)
+        for k in range(nwin):  # Casorati row e is pixel (e % bs, e // bs)
+            u[r0:r0 + bs, c0:c0 + bs, k] = B[:, k].reshape(bs, bs, order="F")
+    u = np.asfortranarray(u / u.max())
+    P = (S - bs + 1) ** 2
+    blk = np.arange(P) % (G * G)
+    rows = np.tile((bs * (blk % G)).astype(np.int32), (nwin, 1))
+    cols = np.tile((bs * (blk // G)).astype(np.int32), (nwin, 1))
+    return u, rows, cols
+
+
+def test_jacobi_fp64_convergence_decisions(capi, oracle):
+    """Near-degenerate singular pairs (equal to within 1e-4) leave inner
+    products at the FP32 rounding level near the rotation threshold; the
+    kernel then decides convergence from FP64 inner products.  The decisions
+    are taken (counted) and the singular values stay within the tolerance of
+    FP64 LAPACK, the pairs' close values included."""
+    u, rows, cols = _near_degenerate_window(17)
+    S1, st = capi.svd_window(u, 4, 1, rows, cols, status=True)
+    S0 = oracle.svd_window(u, 4, 1, rows, cols)
+    S1 = S1.astype(np.float64)
+    err = np.abs(S1 - S0) / S0[:, :1]
+    print("FP64 convergence tests %d over %d matrices, %.2f sweeps per warp, max err %.3g"
+          % (st.svd_fp64_tests, st.svd_matrices, st.svd_warp_sweeps / max(1, st.svd_matrices / 8),
+             err.max()))
+    assert st.svd_fp64_tests > 0
+    assert err.max() < 2e-5
+    # the close pairs are resolved as two values, in order
+    d0 = S0[:, 0] - S0[:, 1]
+    d1 = S1[:, 0] - S1[:, 1]
+    assert np.all(d1 >= 0)
+    assert np.abs(d1 - d0).max() < 2e-5
+
+
+# ---- the lambda search against a dense grid of the oracle's risk
+
+@pytest.mark.parametrize("noise", ["counts", "normalised", "estimated"])
+def test_lambda_search_within_1pct_of_dense_grid(capi, oracle, pkg, noise):
+    """The dense-grid minimum of the FP64 oracle's risk is the arbiter of the
+    search: on sampled windows the GPU's plain search and the learned
+    proposal + narrow search both return a lambda whose oracle risk is within
+    1% of the minimum over 256 lambda values spanning [0, upper].  Noise
+    parameters: the raw counts used on the normalised window (the
+    reference's units, whose risk is smallest at a bound), the same divided
+    by the sequence maximum, and estimated per window."""
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=5, side=64, nt=20)
+    X = noisy.astype(np.float64)
+    if noise == "normalised":
+        a, m, s = a / X.max(), m / X.max(), s / X.max()
+    elif noise == "estimated":
+        a = m = s = -1.0
+    kw = dict(median_size=-1, random_seed=7, alpha=a, mu=m, sigma=s)
+    _, est, _, ex = capi.denoise_ex(X, capi.default_params(**kw))
+    model = pkg.learned.load_model()
+    _, estl, _, exl = capi.denoise_ex(X, capi.default_params(lambda_model=model.ctypes.data, **kw))
+    grid = np.concatenate([[0.0], np.geomspace(1e-4, 100.0, 255)])
+    for t in (7, 10, 19):
+        u = _window(X, t, 7)
+        rows, cols = oracle.arps_window(u, 4, 7, t, 7, 20)
+        na, nm_, ns = est[t, 1], est[t, 2], est[t, 3]  # caller-side values used
+        r = oracle.risk_window(u, 4, 1, rows, cols, np.concatenate([grid, [est[t, 0],
+                               estl[t, 0]]]), na, nm_, ns, 7)
+        rmin, rg, rl = r[:-2].min(), r[-2], r[-1]
+        gp, gl = (rg - rmin) / abs(rmin), (rl - rmin) / abs(rmin)
+        print("%s t=%d grid min %.6g at %.4g; plain %.4g (%d evals) gap %.2e; learned %.4g "
+              "(%d evals) gap %.2e" % (noise, t, rmin, grid[np.argmin(r[:-2])], est[t, 0],
+                                       ex["evals"][t], gp, estl[t, 0], exl["evals"][t], gl))
+        assert gp <= 0.01
+        assert gl <= 0.01

@@ -250,6 +250,32 @@ def test_denoise_threads_do_not_change_results(oracle):
     np.testing.assert_allclose(Y1, g["Y_fixed"], rtol=1e-12, atol=1e-10)
 
 
+def test_window_threads_do_not_change_results(oracle):
+    """Threads inside a window (ARPS positions, SVD patches, reconstruction
+    frames) give the bits of the single-threaded window, PGURE search included."""
+    g = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    kw = dict(traj_length=15, block_size=4, motion_window=7, median_size=-1, random_seed=11,
+              optimize_pgure=1, alpha=a, mu=m, sigma=s, search_points=8, search_rounds=2,
+              frame_begin=6, frame_end=10)
+    Y1, e1, _ = oracle.denoise(g["X"], n_jobs=1, window_threads=1, **kw)
+    Y3, e3, _ = oracle.denoise(g["X"], n_jobs=1, window_threads=3, **kw)
+    np.testing.assert_array_equal(Y1, Y3)
+    np.testing.assert_array_equal(e1, e3)
+    np.testing.assert_allclose(Y1[:, :, 6:10], g["Y_pgure"][:, :, 6:10], rtol=1e-12, atol=1e-10)
+    u = g["u_8"]
+    try:
+        oracle.set_threads(3)
+        r3, c3 = oracle.arps_window(u, 4, 7, 8, 7, 16)
+        S3 = oracle.svd_window(u, 4, 1, r3, c3)
+        v3 = oracle.reconstruct_window(u, 4, 1, r3, c3, 1.0)
+    finally:
+        oracle.set_threads(1)
+    np.testing.assert_array_equal(r3, g["rows_8"])
+    np.testing.assert_array_equal(S3, oracle.svd_window(u, 4, 1, r3, c3))
+    np.testing.assert_array_equal(v3, oracle.reconstruct_window(u, 4, 1, r3, c3, 1.0))
+
+
 @pytest.mark.skipif(not reference_available(), reason="reference test data not mounted")
 def test_reference_fixture_quality_bound(oracle):
     """The reference's end-to-end fixture (pguresvt/tests/test_svt.py:61-106):
