@@ -540,10 +540,12 @@ struct Pgure {
     make_probes(seed, C, d1.data(), d2.data());
     U2p.resize(C);
     U2m.resize(C);
-    for (size_t i = 0; i < C; ++i) {
-      U2p[i] = U[i] + (d2[i] * eps2);
-      U2m[i] = U[i] - (d2[i] * eps2);
-    }
+    par_chunks(C, threads, [&](size_t b, size_t e, uint32_t) {
+      for (size_t i = b; i < e; ++i) {
+        U2p[i] = U[i] + (d2[i] * eps2);
+        U2m[i] = U[i] - (d2[i] * eps2);
+      }
+    });
     if (!intDelta1) {
       U1.resize(C);
       for (size_t i = 0; i < C; ++i) U1[i] = U[i] + (d1[i] * eps1);
@@ -568,13 +570,24 @@ struct Pgure {
     const size_t C = g.cube();
     const double OoN = 1.0 / (g.S * g.S * g.nwin);
     const double* u = U;
-    const double t1 = accu2(C, [&](size_t i) { const double d = std::fabs(Uhat[i] - u[i]); return d * d; });
-    const double t2 = accu2(C, [&](size_t i) { return u[i]; });
-    const double t3 = accu2(C, [&](size_t i) {
-      return (double)d1[i] * ((alpha * u[i] - alpha * mu) + sigmasq) * (R1[i] - Uhat[i]);
+    // the five sums, each in accu()'s order; with several threads each sum
+    // runs on its own thread (the same additions, so the same bits)
+    double t[5];
+    auto sum = [&](size_t which) {
+      switch (which) {
+        case 0: t[0] = accu2(C, [&](size_t i) { const double d = std::fabs(Uhat[i] - u[i]); return d * d; }); break;
+        case 1: t[1] = accu2(C, [&](size_t i) { return u[i]; }); break;
+        case 2: t[2] = accu2(C, [&](size_t i) {
+                  return (double)d1[i] * ((alpha * u[i] - alpha * mu) + sigmasq) * (R1[i] - Uhat[i]);
+                }); break;
+        case 3: t[3] = accu2(C, [&](size_t i) { return d2[i] * ((R2p[i] - 2 * Uhat[i]) + R2m[i]); }); break;
+        default: t[4] = accu2(C, [&](size_t i) { return Uhat[i]; }); break;
+      }
+    };
+    par_chunks(5, svt0.threads, [&](size_t b, size_t e, uint32_t) {
+      for (size_t k = b; k < e; ++k) sum(k);
     });
-    const double t4 = accu2(C, [&](size_t i) { return d2[i] * ((R2p[i] - 2 * Uhat[i]) + R2m[i]); });
-    const double t5 = accu2(C, [&](size_t i) { return Uhat[i]; });
+    const double t1 = t[0], t2 = t[1], t3 = t[2], t4 = t[3], t5 = t[4];
     return OoN * (t1 - (alpha + mu) * t2 + (2 / eps1 * t3) -
                   (2 * sigmasq * alpha / (eps2 * eps2) * t4) + (2 * mu * t5) + mu) -
            sigmasq;

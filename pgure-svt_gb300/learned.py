@@ -48,6 +48,44 @@ def random_sequence(seed, estimated=False):
     return np.asfortranarray(noisy.astype(np.float32)), (None if estimated else (alpha, mu, sigma))
 
 
+HELDOUT_SIDE = 512
+HELDOUT_FRAMES = 200
+HELDOUT_OUTPUTS = (7, 66, 133, 192)  # output frames whose full windows are evaluated
+
+
+def heldout_windows(seed, estimated=False):
+    """The sampled windows of one held-out 512x512x200 sequence: the same
+    scene distribution as random_sequence (blob or blob+lattice, integer or
+    sub-pixel drift over all 200 frames, alpha in [0.05, 1], mu in [0, 2],
+    sigma in [0.5, 5]), rendered only on the 15-frame windows of the output
+    frames HELDOUT_OUTPUTS (frame noise seeded per frame).  Returns a list of
+    (noisy float32 window, clean window) and the noise parameters (None with
+    `estimated`).  Output frame 7 of a window array is the window's centre,
+    a middle window exactly as in the whole sequence."""
+    rng = np.random.default_rng(seed)
+    side, nt = HELDOUT_SIDE, HELDOUT_FRAMES
+    nblobs = max(1, int(round(300 * rng.uniform(0.3, 1.5))))
+    lattice = bool(rng.random() < 0.5)
+    integer = bool(rng.random() < 0.3)
+    max_step = 1 if integer else float(rng.uniform(0.0, 2.0))
+    alpha = float(rng.uniform(0.05, 1.0))
+    mu = float(rng.uniform(0.0, 2.0))
+    sigma = float(rng.uniform(0.5, 5.0))
+    scene = int(rng.integers(1 << 31))
+    noise_seed = int(rng.integers(1 << 31))
+    frames = [f for t in HELDOUT_OUTPUTS for f in range(t - 7, t + 8)]
+    clean = synth.blobs(side, nt, nblobs, scene, max_step, integer, lattice, frames=frames)
+    out = []
+    for w, t in enumerate(HELDOUT_OUTPUTS):
+        cw = np.asfortranarray(clean[:, :, 15 * w:15 * (w + 1)])
+        nw = np.empty_like(cw)
+        for k in range(15):
+            nw[:, :, k] = synth.poisson_gaussian(cw[:, :, k:k + 1], alpha, mu, sigma,
+                                                 noise_seed + t - 7 + k)[:, :, 0]
+        out.append((np.asfortranarray(nw.astype(np.float32)), cw))
+    return out, (None if estimated else (alpha, mu, sigma))
+
+
 def search_params(noise, frames=None, model=None, **kw):
     """Parameters of the benchmark's PGURE search (4x4 patches, T=15,
     motion window 7, reference compat mode, probe seed 7) with the given

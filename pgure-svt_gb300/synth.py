@@ -44,11 +44,14 @@ def _drift(rng, nt, max_step, integer):
 
 
 def blobs(side, nt, nblobs, seed, max_step=1.0, integer_drift=True, lattice=False,
-          background=5.0):
+          background=5.0, frames=None):
     """Clean (side, side, nt) float64 sequence, column-major like the reference.
 
     Isotropic Gaussians are separable, so a frame is background +
     Gy diag(peak) Gx^T with Gy[y, b] = exp(-(y - cy_b)^2 / 2s_b^2) (same for x).
+    `frames` (indices into the nt-frame sequence) renders only those frames,
+    in that order, with the drift of the whole sequence; the lattice
+    amplitude then follows the rendered frames' mean.
     """
     rng = np.random.default_rng(seed)
     cy = rng.uniform(0, side, nblobs)
@@ -57,22 +60,23 @@ def blobs(side, nt, nblobs, seed, max_step=1.0, integer_drift=True, lattice=Fals
     pk = rng.uniform(20.0, 200.0, nblobs)
     off = _drift(rng, nt, max_step, integer_drift)
     r = np.arange(side, dtype=float)[:, None]
-    X = np.empty((side, side, nt), dtype=float, order="F")
+    ts = list(range(nt)) if frames is None else [int(t) for t in frames]
+    X = np.empty((side, side, len(ts)), dtype=float, order="F")
     if lattice:
         period = rng.uniform(6.0, 10.0, 2)
         phase = rng.uniform(0, 2 * np.pi, 2)
-    for t in range(nt):
+    for n, t in enumerate(ts):
         dy, dx = off[t]
         gy = np.exp(-((r - cy[None, :] - dy) ** 2) / (2 * sg[None, :] ** 2))
         gx = np.exp(-((r - cx[None, :] - dx) ** 2) / (2 * sg[None, :] ** 2))
-        X[:, :, t] = background + gy @ (pk[:, None] * gx.T)
+        X[:, :, n] = background + gy @ (pk[:, None] * gx.T)
     if lattice:
         amp = 0.15 * X.mean()
-        for t in range(nt):
+        for n, t in enumerate(ts):
             dy, dx = off[t]
             ly = np.sin(2 * np.pi * (r[:, 0] - dy) / period[0] + phase[0])
             lx = np.sin(2 * np.pi * (r[:, 0] - dx) / period[1] + phase[1])
-            X[:, :, t] += amp * np.outer(ly, lx)
+            X[:, :, n] += amp * np.outer(ly, lx)
         np.maximum(X, 0.0, out=X)
     return X
 

@@ -48,6 +48,75 @@ def _gen_est(seed):
     return _package().learned.random_sequence(seed, estimated=True)
 
 
+def _gen_heldout(seed):
+    return _package().learned.heldout_windows(seed)
+
+
+def _gen_heldout_est(seed):
+    return _package().learned.heldout_windows(seed, estimated=True)
+
+
+GRID = np.concatenate([[0.0], np.geomspace(1e-4, 100.0, 255)])  # 256 values over [0, upper]
+
+
+def grid_risks(pkg, X, noise):
+    """The PGURE risk of the window centre (frame 7 of X) at every GRID
+    value: 16 copies of the window, 16 fixed lambda values each, in one
+    pgsvt_denoise_batch call."""
+    L, C = pkg.learned, pkg._capi
+    seqs = [dict(X=X, params=L.search_params(noise, (7, 8)), lambdas=GRID[16 * i:16 * (i + 1)])
+            for i in range(16)]
+    res, _ = C.denoise_batch(seqs)
+    return np.concatenate([r["risks"][7] for r in res])
+
+
+def evaluate_512(pkg, model, seeds, pool, estimated=False):
+    """Held-out 512x512x200 sequences (config 5's evaluation set): for each
+    sampled window, the plain search and the learned proposal + narrow
+    search, their risk against the minimum over a 256-value lambda grid (the
+    arbiter), risk evaluations and the PSNR of the denoised centre frame."""
+    L = pkg.learned
+    rows = []
+    mdl = np.ascontiguousarray(model, np.float32)
+    t0 = time.time()
+    for wins, noise in pool.imap(_gen_heldout_est if estimated else _gen_heldout, seeds):
+        for X, clean in wins:
+            res = L.compare(X, noise, mdl, frames=(7, 8))
+            g = grid_risks(pkg, X, noise)
+            gmin = float(g.min())
+            c = clean[:, :, 7]
+            peak = float(clean.max())
+            row = dict(grid_min=gmin, grid_argmin=float(GRID[int(np.argmin(g))]))
+            for name in ("plain", "learned"):
+                r = res[name]
+                y = r["Y"][:, :, 7]
+                row[name] = dict(lam=float(r["lambdas"][7]), risk=float(r["risk"][7]),
+                                 evals=int(r["evals"][7]),
+                                 gap_grid=float((r["risk"][7] - gmin) / abs(gmin)),
+                                 psnr=float(10 * np.log10(peak ** 2 / np.mean((c - y) ** 2))))
+            rp, rl = row["plain"]["risk"], row["learned"]["risk"]
+            row["gap_learned_vs_plain"] = float((rl - rp) / abs(rp))
+            rows.append(row)
+    def col(a, b):
+        return np.array([r[a][b] for r in rows])
+    gap = np.array([r["gap_learned_vs_plain"] for r in rows])
+    out = dict(sequences=len(seeds), windows=len(rows), seconds=time.time() - t0,
+               outputs=list(L.HELDOUT_OUTPUTS), grid="0 and 255 log-spaced values in [1e-4, 100]",
+               gap_learned_vs_plain_max=float(gap.max()), gap_learned_vs_plain_mean=float(gap.mean()),
+               frac_learned_vs_plain_le_1pct=float(np.mean(gap <= 0.01)))
+    for name in ("plain", "learned"):
+        gg = col(name, "gap_grid")
+        out[name] = dict(evals_mean=float(col(name, "evals").mean()),
+                         gap_grid_max=float(gg.max()), gap_grid_mean=float(gg.mean()),
+                         frac_gap_grid_le_1pct=float(np.mean(gg <= 0.01)),
+                         psnr_mean=float(col(name, "psnr").mean()))
+    out["psnr_delta_learned_minus_plain_db"] = dict(
+        mean=float((col("learned", "psnr") - col("plain", "psnr")).mean()),
+        min=float((col("learned", "psnr") - col("plain", "psnr")).min()),
+        max=float((col("learned", "psnr") - col("plain", "psnr")).max()))
+    return out
+
+
 def evaluate(pkg, model, seeds, pool, estimated=False):
     """Held-out windows: prediction error, plain vs learned search."""
     L = pkg.learned
@@ -91,6 +160,9 @@ def main():
     ap.add_argument("--report", default=None)
     ap.add_argument("--evaluate", default=None,
                     help="only evaluate this model on the held-out sequences")
+    ap.add_argument("--held-out-512", type=int, default=0,
+                    help="with --evaluate: also this many held-out 512x512x200 sequences "
+                         "(4 sampled windows each), given and estimated noise")
     a = ap.parse_args()
 
     pool = mp.get_context("spawn").Pool(a.workers)  # before any GPU call
@@ -107,6 +179,12 @@ def main():
 
     if a.evaluate:
         ev = evaluate_both(L.load_model(a.evaluate))
+        if a.held_out_512:
+            mdl = L.load_model(a.evaluate)
+            s512 = [3 * 10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out_512)]
+            ev["held_out_512"] = evaluate_512(pkg, mdl, s512, pool)
+            s512 = [4 * 10 ** 6 + a.seed * 1000003 + i for i in range(a.held_out_512)]
+            ev["held_out_512_estimated"] = evaluate_512(pkg, mdl, s512, pool, estimated=True)
         pool.close()
         pool.join()
         print(json.dumps(ev))

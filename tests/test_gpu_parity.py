@@ -335,20 +335,23 @@ def test_large_patches_match_oracle(capi, oracle, pkg, bs, T, ov):
 
 def _near_degenerate_window(seed, G=8, bs=4, nwin=15):
     """A window whose kept patches' Casorati matrices are designed: G x G
-    disjoint bs x bs blocks, block b holding B_b = U diag(s) V^T (random
-    orthonormal U, V) with three pairs of singular values equal to within
-    1e-6..1e-4 relative, and a trajectory table sending every position to a
-    block.  Returns (u, rows, cols)."""
+    disjoint bs x bs blocks, and a trajectory table sending every position
+    to a block.  Block b holds orthogonal columns a_k = s_k u_k (random
+    orthonormal u_k) in which three pairs have equal norms (s_1 = s_0,
+    s_5 = s_4, s_10 = s_9) and are coupled, a_j += d s_j u_i with d in
+    [1.5e-6, 3.5e-6]: a first sweep finds only these near-degenerate pairs,
+    with inner products between the rotation threshold (1e-6) and four times
+    it.  Returns (u, rows, cols)."""
     rng = np.random.default_rng(seed)
     m, S = bs * bs, bs * G
     u = np.zeros((S, S, nwin))
     for b in range(G * G):
         Uq, _ = np.linalg.qr(rng.standard_normal((m, nwin)))
-        Vq, _ = np.linalg.qr(rng.standard_normal((nwin, nwin)))
         s = np.sort(rng.uniform(0.05, 1.0, nwin))[::-1]
+        B = Uq * s
         for i in (0, 4, 9):
-            s[i + 1] = s[i] * (1.0 - rng.uniform(1e-6, 1e-4))
-        B = Uq @ np.diag(s) @ Vq.T
+            s[i + 1] = s[i]
+            B[:, i + 1] = s[i] * (Uq[:, i + 1] + rng.uniform(1.5e-6, 3.5e-6) * Uq[:, i])
         r0, c0 = bs * (b % G), bs * (b // G)
         for k in range(nwin):  # Casorati row e is pixel (e % bs, e // bs)
             u[r0:r0 + bs, c0:c0 + bs, k] = B[:, k].reshape(bs, bs, order="F")
@@ -361,11 +364,12 @@ def _near_degenerate_window(seed, G=8, bs=4, nwin=15):
 
 
 def test_jacobi_fp64_convergence_decisions(capi, oracle):
-    """Near-degenerate singular pairs (equal to within 1e-4) leave inner
-    products at the FP32 rounding level near the rotation threshold; the
-    kernel then decides convergence from FP64 inner products.  The decisions
-    are taken (counted) and the singular values stay within the tolerance of
-    FP64 LAPACK, the pairs' close values included."""
+    """Near-degenerate singular pairs whose inner products sit at the FP32
+    noise level of the rotation threshold: when a sweep's only rotations are
+    of such pairs, the kernel decides convergence from FP64 inner products of
+    the FP32 entries.  The decisions are taken (counted) and the singular
+    values stay within the tolerance of FP64 LAPACK, the pairs' close values
+    included."""
     u, rows, cols = _near_degenerate_window(17)
     S1, st = capi.svd_window(u, 4, 1, rows, cols, status=True)
     S0 = oracle.svd_window(u, 4, 1, rows, cols)

@@ -354,3 +354,72 @@ def test_median_restatement_matches_live_reference(oracle):
         ref = np.zeros_like(a, order="F")
         L.ref_median_filter(a.ctypes.data, ref.ctypes.data, S, S, r)
         np.testing.assert_array_equal(oracle.median_filter(a, r), ref)
+
+
+# ---- Q6: the reference returns the search's last evaluation, not its best
+
+def _nelder_mead_1d(f, x0, step, lo, hi, ftol, maxeval):
+    """A two-vertex Nelder-Mead simplex (Nelder & Mead 1965; reflection 1,
+    expansion 2, contraction 1/2) on [lo, hi], stopped when the vertices'
+    values agree to ftol relative, the rule NLopt's ftol_rel applies.
+    Returns (best (x, f), last evaluated (x, f), evaluations)."""
+    clamp = lambda x: min(max(x, lo), hi)  # noqa: E731
+    hist = []
+
+    def ev(x):
+        v = f(x)
+        hist.append((x, v))
+        return v
+
+    xs = [clamp(x0), clamp(x0 + step)]
+    fs = [ev(xs[0]), ev(xs[1])]
+    while len(hist) < maxeval:
+        b, w = (0, 1) if fs[0] <= fs[1] else (1, 0)
+        if abs(fs[w] - fs[b]) <= ftol * abs(fs[b]) or xs[w] == xs[b]:
+            break
+        xr = clamp(2 * xs[b] - xs[w])
+        fr = ev(xr)
+        if fr < fs[b]:
+            xe = clamp(3 * xs[b] - 2 * xs[w])
+            fe = ev(xe)
+            xs[w], fs[w] = (xe, fe) if fe < fr else (xr, fr)
+        elif fr < fs[w]:
+            xs[w], fs[w] = xr, fr
+        else:
+            xc = xs[b] + 0.5 * (xs[w] - xs[b])
+            fc = ev(xc)
+            xs[w], fs[w] = xc, fc
+    best = min(hist, key=lambda t: t[1])
+    return best, hist[-1], len(hist)
+
+
+def test_q6_last_evaluation_versus_best_point(oracle):
+    """The reference returns the last lambda its simplex search evaluated
+    (pgure.hpp:128,236), the library the best one.  With a simplex search
+    stopped on ftol_rel (the reference's tol = 1e-7, initial step sqrt(start),
+    pgure.hpp:206-214) the two differ in risk by about tol: the choice of
+    returned point changes the result far less than the 1% risk gap the
+    parity tests allow.  The library's grid search reaches the simplex's
+    best risk within that gap."""
+    g = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    X = g["X"].astype(np.float64)
+    # noise parameters in the normalised window's units: an interior optimum
+    a, m, s = (float(g[k]) / X.max() for k in ("alpha", "mu", "sigma"))
+    for t in (4, 8, 12):
+        s0 = t - 7 if 7 <= t < 9 else (0 if t < 7 else 1)
+        u = X[:, :, s0:s0 + 15]
+        u = u / u.max()
+        rows, cols = oracle.arps_window(u, 4, 7, t, 7, 16)
+        f = lambda lam: float(oracle.risk_window(u, 4, 1, rows, cols, [lam], a, m, s, 11)[0])  # noqa: E731
+        start = float(np.mean(u))
+        upper = max(100.0, start)
+        (xb, fb), (xl, fl), n = _nelder_mead_1d(f, start, np.sqrt(start), 0.0, upper, 1e-7, 500)
+        _, est, rep = oracle.denoise(X, n_jobs=1, random_seed=11, alpha=a, mu=m, sigma=s,
+                                     frame_begin=t, frame_end=t + 1)
+        fg = f(est[t, 0])
+        print("t=%d simplex: %d evals, best %.6g (lambda %.4g), last %.6g (lambda %.4g), "
+              "last-best %.2e rel; grid search %.6g (lambda %.4g, %d evals)"
+              % (t, n, fb, xb, fl, xl, (fl - fb) / abs(fb), fg, est[t, 0], rep.risk_evals))
+        assert fb <= fl
+        assert (fl - fb) / abs(fb) <= 1e-3
+        assert (fg - fb) / abs(fb) <= 0.01
