@@ -158,7 +158,8 @@ typedef struct {
   uint64_t svd_launches;    /* launches of the SVD kernel                 */
   uint64_t svd_matrices;    /* Casorati matrices decomposed               */
   uint64_t arps_exact_steps;/* ARPS diamond steps decided in FP64         */
-  uint64_t svd_fp64_tests;  /* Jacobi convergence tests decided in FP64   */
+  uint64_t svd_fp64_tests;  /* Jacobi convergence decisions taken from    *
+                             * FP64 inner products (per patch and check)  */
   uint64_t svd_warp_sweeps; /* Jacobi sweeps summed over warps            */
   char message[256];        /* human-readable error / note                */
   int32_t svd_variant;      /* SVD kernel shape used (0: default)         */
@@ -308,7 +309,7 @@ int pgsvt_svd_window(const double* u, uint32_t nrows, uint32_t nwin,
 
 /* pgsvt_svd_window that also fills `st` (may be NULL): svd_matrices,
  * svd_warp_sweeps and svd_fp64_tests, the Jacobi convergence decisions taken
- * from FP64 inner products on near-degenerate singular pairs.              */
+ * from FP64 inner products when a sweep rotated only near-degenerate pairs. */
 int pgsvt_svd_window_ex(const double* u, uint32_t nrows, uint32_t nwin,
                         uint32_t block_size, uint32_t block_overlap,
                         const int32_t* rows, const int32_t* cols, float* S,

@@ -600,7 +600,9 @@ struct Pgure {
 // [lo, hi]; each later round evaluates K points evenly inside the bracket
 // formed by the neighbours of the best point so far.  Returns the best point
 // (ties: smallest lambda).  Stops early when a round improves the best risk by
-// no more than tol*|risk|, or when max_eval is reached.
+// no more than tol*|risk| while the bracket is narrower than kNarrowBracket
+// times the best point, or when max_eval is reached.
+constexpr double kNarrowBracket = 0.25;
 
 struct SearchResult {
   double lambda, risk;
@@ -656,7 +658,10 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
     b = best_of();
     res.lambda = pts[b].l;
     res.risk = pts[b].r;
-    if (prev - pts[b].r <= tol * std::fabs(pts[b].r)) break;
+    const double nlo = (b > 0) ? pts[b - 1].l : (include_zero_lo ? 0.0 : pts[b].l);
+    const double nhi = (b + 1 < pts.size()) ? pts[b + 1].l : pts[b].l;
+    if (prev - pts[b].r <= tol * std::fabs(pts[b].r) && nhi - nlo <= kNarrowBracket * pts[b].l)
+      break;  // no progress and a narrow bracket
   }
   res.evals = evals;
   return res;

@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
   s.nnext = 0;
   const int b = Sch::best(s);
   s.best = b;
+  const bool grid_round = s.first != 0;
   if (s.first) {
     s.first = 0;
     const bool bound = (b == 0 && s.zero_lo) || (b == s.npts - 1 && s.lam[b] >= wc.upper);
@@ -280,17 +281,18 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
     }
   } else {
     ++s.rd;
-    if (prev_best - s.risk[b] <= pb.tol * fabs(s.risk[b])) {
-      search_finish(s, d.counters);
-      return;
-    }
+  }
+  const double blo = (b > 0) ? s.lam[b - 1] : (s.zero_lo ? 0.0 : s.lam[b]);
+  const double bhi = (b + 1 < s.npts) ? s.lam[b + 1] : s.lam[b];
+  if (!grid_round && prev_best - s.risk[b] <= pb.tol * fabs(s.risk[b]) &&
+      bhi - blo <= kNarrowBracket * s.lam[b]) {
+    search_finish(s, d.counters);  // no progress and a narrow bracket
+    return;
   }
   if (s.rd >= s.rounds || s.evals_phase + s.K > s.max_eval) {
     search_finish(s, d.counters);
     return;
   }
-  const double blo = (b > 0) ? s.lam[b - 1] : (s.zero_lo ? 0.0 : s.lam[b]);
-  const double bhi = (b + 1 < s.npts) ? s.lam[b + 1] : s.lam[b];
   if (!(bhi > blo)) {
     search_finish(s, d.counters);
     return;

@@ -54,6 +54,10 @@ inline std::vector<int32_t> kept_patches(int S, int bs, int ov) {
 
 constexpr int kMaxK = 16;          // lambda values per evaluation round
 constexpr int kMaxPts = 160;       // evaluated points kept per window
+// The lambda search stops after a refinement round without progress only
+// when the bracket around its best point is narrower than this fraction of
+// the point (else it refines again, within its round and evaluation limits).
+constexpr double kNarrowBracket = 0.25;
 constexpr int kMaxMW = 15;         // motion window supported by ARPS
 constexpr int kEvalPatches = 64;   // kept patches per lambda-evaluation block (8 x 8 tile)
 constexpr double kFixScale = 4294967296.0;  // 2^32 fixed-point scale

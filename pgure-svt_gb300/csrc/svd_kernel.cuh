@@ -202,9 +202,11 @@ constexpr int svd_minblocks() {
 // Only near-degenerate pairs moved, by amounts at the FP32 noise level of
 // their inner products: decide convergence from FP64 inner products of the
 // current columns (exact products of the FP32 entries) staged in As
-// ([NC][CS], this lane's RPL rows at q * RPL).
+// ([NC][CS], this lane's RPL rows at q * RPL).  fp64_tests counts these
+// decisions (one per patch and check).
 template <int RPL, int LANES, int CS>
 __device__ bool fp64_check(const float* As, int q, int nwin, unsigned& fp64_tests) {
+  ++fp64_tests;
   bool again = false;
   for (int i = 0; i < nwin; ++i) {
     for (int j = i + 1; j < nwin; ++j) {
@@ -227,10 +229,7 @@ __device__ bool fp64_check(const float* As, int q, int nwin, unsigned& fp64_test
         for (int r = 0; r < RPL; ++r)
           g64 = fma((double)As[i * CS + q * RPL + r], (double)As[j * CS + q * RPL + r], g64);
         g64 = lanes_sum_d<LANES>(g64);
-        if (cand) {
-          ++fp64_tests;
-          if (fabs(g64) > (double)kTol * (double)sc) again = true;
-        }
+        if (cand && fabs(g64) > (double)kTol * (double)sc) again = true;
       }
     }
   }
@@ -238,13 +237,145 @@ __device__ bool fp64_check(const float* As, int q, int nwin, unsigned& fp64_test
   return __any_sync(0xffffffffu, again);
 }
 
+// Patches of 4 lanes x 4 rows and at most 16 columns take the owner form of
+// the sweeps (below), unrolled three rounds per loop iteration where the
+// round count allows (PGSVT_SVD_OWNER_UNROLL).
+template <int RPL, int LANES, int NC>
+constexpr bool kOwnerForm =
+#ifdef PGSVT_SVD_REPLICATED
+    false;
+#else
+    RPL == 4 && LANES == 4 && NC <= 16;
+#endif
+#ifndef PGSVT_SVD_OWNER_UNROLL
+#define PGSVT_SVD_OWNER_UNROLL 3
+#endif
+template <int NC>
+constexpr int kOwnerUnroll = ((NC - 1) % PGSVT_SVD_OWNER_UNROLL == 0) ? PGSVT_SVD_OWNER_UNROLL : 1;
+
+// Lane q's copy of one of four per-lane candidates (q = 0..3), from registers
+// with compile-time indices.
+__device__ __forceinline__ float sel4(int q, float a, float b, float c, float d) {
+  return (q & 2) ? ((q & 1) ? d : c) : ((q & 1) ? b : a);
+}
+
+// Jacobi sweeps for patches held by 4 lanes x 4 rows, with each pair's
+// rotation computed once per patch instead of in all four lanes.  The lanes
+// reduce-scatter the round's inner products (two exchange steps) so that lane
+// q holds the complete inner products of pairs q and q + 4 (pair 0 is the
+// zero pad column's); it computes those pairs' rotations and rotated norms
+// and broadcasts them, and every lane applies every rotation to its rows.
+// The pairs, the rotation formulas and the convergence rules are those of
+// register_sweeps; pairs no patch of the warp needs to rotate are skipped
+// warp-uniformly (a patch that does not need a rotated pair applies the
+// identity, which leaves its columns and norms unchanged).
+template <int NC, int CS, int U>
+__device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
+                            unsigned& fp64_tests) {
+  constexpr int NP = NC / 2;  // pairs per round, pair 0 included
+  static_assert(NP <= 8, "each lane owns two pairs");
+  const int gbase = (threadIdx.x & 31) & ~3;
+  const bool b1 = (q & 2) != 0, b0 = (q & 1) != 0;
+  int sweeps = 0;
+  float nrm[NC];
+#pragma unroll 1
+  for (; sweeps < kMaxSweeps; ++sweeps) {
+#pragma unroll
+    for (int k = 0; k < NC - 1; ++k) {
+      float s = 0.f;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) s = fmaf(A(r, k), A(r, k), s);
+      nrm[k] = lanes_sum<4>(s);
+    }
+    nrm[NC - 1] = 0.f;
+    bool definite = false, band = false;
+#pragma unroll U
+    for (int rd = 0; rd < NC - 1; ++rd) {
+      // this lane's partial inner products of the round's pairs
+      float gm[8];
+#pragma unroll
+      for (int pp = 0; pp < 8; ++pp) {
+        if (pp >= 1 && pp < NP) {
+          float2 t = __fmul2_rn(A.v[0][pp], A.v[0][NC - 1 - pp]);
+          t = __ffma2_rn(A.v[1][pp], A.v[1][NC - 1 - pp], t);
+          gm[pp] = t.x + t.y;
+        } else {
+          gm[pp] = 0.f;
+        }
+      }
+      // reduce-scatter: across lanes q, q^2 keep the pairs whose bit 1 is
+      // q's (pp = 2*b1 + {0, 1, 4, 5}), then across q, q^1 those whose bit
+      // 0 is q's: gv[i] is the inner product of pair q + 4i
+      float h[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int lo = (j & 1) | ((j >> 1) << 2);
+        const float keep = b1 ? gm[lo + 2] : gm[lo];
+        const float send = b1 ? gm[lo] : gm[lo + 2];
+        h[j] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+      }
+      float cs_[2], sn_[2], ni_[2], nj_[2];
+      bool need_[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float keep = b0 ? h[2 * i + 1] : h[2 * i];
+        const float send = b0 ? h[2 * i] : h[2 * i + 1];
+        const float gv = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+        const int po = q + 4 * i;  // the owned pair
+        const float al = sel4(q, nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2], nrm[4 * i + 3]);
+        const float be = sel4(q, nrm[NC - 1 - 4 * i], nrm[NC - 2 - 4 * i], nrm[NC - 3 - 4 * i],
+                              nrm[NC - 4 - 4 * i]);
+        const float g2 = gv * gv, ab = al * be;
+        need_[i] = po >= 1 && po < NP && g2 > (kTol * kTol) * ab;
+        cs_[i] = 1.f;
+        sn_[i] = 0.f;
+        ni_[i] = al;
+        nj_[i] = be;
+        if (need_[i]) {
+          rotation(al, be, gv, g2, ab, cs_[i], sn_[i], definite, band);
+          rotated_norms(al, be, gv, cs_[i], sn_[i], ni_[i], nj_[i]);
+        }
+      }
+      const unsigned m0 = __ballot_sync(0xffffffffu, need_[0]);
+      const unsigned m1 = __ballot_sync(0xffffffffu, need_[1]);
+#pragma unroll
+      for (int pp = 1; pp < NP; ++pp) {
+        const int i = pp >> 2;
+        if (!((i ? m1 : m0) & (0x11111111u << (pp & 3)))) continue;  // warp-uniform
+        const int src = gbase | (pp & 3);
+        const float cs = __shfl_sync(0xffffffffu, cs_[i], src);
+        const float sn = __shfl_sync(0xffffffffu, sn_[i], src);
+        const float ni = __shfl_sync(0xffffffffu, ni_[i], src);
+        const float nj = __shfl_sync(0xffffffffu, nj_[i], src);
+        A.rotate(pp, NC - 1 - pp, cs, sn);
+        nrm[pp] = ni;
+        nrm[NC - 1 - pp] = nj;
+      }
+      A.shift();
+      shift_norms<NC>(nrm);
+    }
+    if (__any_sync(0xffffffffu, definite)) continue;
+    if (!__any_sync(0xffffffffu, band)) break;
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) As[k * CS + q * 4 + r] = A(r, k);
+    __syncwarp();
+    if (!fp64_check<4, 4, CS>(As, q, nwin, fp64_tests)) break;
+  }
+  return sweeps;
+}
+
 // Jacobi sweeps with the columns in registers: the round-robin moves them one
 // position per round.  Column norms are recomputed exactly at every sweep's
 // start and updated in closed form after each rotation.  Returns the sweeps
 // with rotations; As ([NC][CS]) stages the columns for the FP64 check.
+// Patches of 4 lanes x 4 rows take the owner form above.
 template <int RPL, int LANES, int NC, int CS, int U>
 __device__ int register_sweeps(RegCols<RPL, NC>& A, float* As, int q, int nwin,
                                unsigned& fp64_tests) {
+  if constexpr (kOwnerForm<RPL, LANES, NC>)
+    return owner_sweeps<NC, CS, kOwnerUnroll<NC>>(A, As, q, nwin, fp64_tests);
   int sweeps = 0;
   float nrm[NC];
 #pragma unroll 1
@@ -421,6 +552,73 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
           for (int r = 0; r < RPL; ++r) s = fmaf(va[pp][r], vb[pp][r], s);
           gm[pp] = s;
         }
+        if constexpr (kOwnerForm<RPL, LANES, NC>) {
+          // the owner form's order of operations (owner_sweeps): packed
+          // partial products, the reduce-scatter, one rotation per pair
+          // computed by its owner lane and broadcast; identical results
+#pragma unroll
+          for (int pp = 1; pp < NC / 2; ++pp) {
+            float p0 = va[pp][0] * vb[pp][0], p1 = va[pp][1] * vb[pp][1];
+            p0 = fmaf(va[pp][2], vb[pp][2], p0);
+            p1 = fmaf(va[pp][3], vb[pp][3], p1);
+            gm[pp] = p0 + p1;
+          }
+          float g8[8];
+#pragma unroll
+          for (int pp = 0; pp < 8; ++pp) g8[pp] = (pp >= 1 && pp < NC / 2) ? gm[pp] : 0.f;
+          const bool b1 = (q & 2) != 0, b0 = (q & 1) != 0;
+          float h[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int lo = (j & 1) | ((j >> 1) << 2);
+            const float keep = b1 ? g8[lo + 2] : g8[lo];
+            const float send = b1 ? g8[lo] : g8[lo + 2];
+            h[j] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+          }
+          float cs_[2], sn_[2];
+          bool need_[2];
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const float keep = b0 ? h[2 * i + 1] : h[2 * i];
+            const float send = b0 ? h[2 * i] : h[2 * i + 1];
+            const float gv = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+            const int po = q + 4 * i;
+            int ia = po + rd, ib = NC - 1 - po + rd;
+            if (ia >= NC - 1) ia -= NC - 1;
+            if (ib >= NC - 1) ib -= NC - 1;
+            const bool valid = po >= 1 && po < NC / 2;
+            const float al = valid ? nrs[ia] : 0.f, be = valid ? nrs[ib] : 0.f;
+            const float g2 = gv * gv, ab = al * be;
+            need_[i] = valid && g2 > (kTol * kTol) * ab;
+            cs_[i] = 1.f;
+            sn_[i] = 0.f;
+            if (need_[i]) {
+              rotation(al, be, gv, g2, ab, cs_[i], sn_[i], definite, band);
+              float ni, nj;
+              rotated_norms(al, be, gv, cs_[i], sn_[i], ni, nj);
+              nrs[ia] = ni;
+              nrs[ib] = nj;
+            }
+          }
+          const unsigned m0 = __ballot_sync(0xffffffffu, need_[0]);
+          const unsigned m1 = __ballot_sync(0xffffffffu, need_[1]);
+          const int gbase = lane & ~3;
+#pragma unroll
+          for (int pp = 1; pp < NC / 2; ++pp) {
+            const int i = pp >> 2;
+            if (!((i ? m1 : m0) & (0x11111111u << (pp & 3)))) continue;  // warp-uniform
+            const float cs = __shfl_sync(0xffffffffu, cs_[i], gbase | (pp & 3));
+            const float sn = __shfl_sync(0xffffffffu, sn_[i], gbase | (pp & 3));
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) {
+              const float a = va[pp][r], b = vb[pp][r];
+              va[pp][r] = fmaf(cs, a, -sn * b);
+              vb[pp][r] = fmaf(sn, a, cs * b);
+            }
+            store_rows<RPL>(As + ca[pp] * CS + q * RPL, va[pp]);
+            store_rows<RPL>(As + cb[pp] * CS + q * RPL, vb[pp]);
+          }
+        } else {
 #pragma unroll
         for (int o = 1; o < LANES; o <<= 1)
 #pragma unroll
@@ -449,6 +647,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
               nrs[cb[pp]] = nj;
             }
           }
+        }
         }
         __syncwarp();
       }
