@@ -275,19 +275,32 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
   constexpr int NP = NC / 2;  // pairs per round, pair 0 included
   static_assert(NP <= 8, "each lane owns two pairs");
   const int gbase = (threadIdx.x & 31) & ~3;
+  const int up = gbase | ((q + 1) & 3), dn = gbase | ((q + 3) & 3);
   const bool b1 = (q & 2) != 0, b0 = (q & 1) != 0;
   int sweeps = 0;
-  float nrm[NC];
 #pragma unroll 1
   for (; sweeps < kMaxSweeps; ++sweeps) {
+    // squared norms of the owned pairs' columns: L[i] of position q + 4i,
+    // R[i] of position NC - 1 - q - 4i (the pad column's is 0)
+    float L[2], R[2];
+    {
+      float nrm[NC];
 #pragma unroll
-    for (int k = 0; k < NC - 1; ++k) {
-      float s = 0.f;
+      for (int k = 0; k < NC - 1; ++k) {
+        float t = 0.f;
 #pragma unroll
-      for (int r = 0; r < 4; ++r) s = fmaf(A(r, k), A(r, k), s);
-      nrm[k] = lanes_sum<4>(s);
+        for (int r = 0; r < 4; ++r) t = fmaf(A(r, k), A(r, k), t);
+        nrm[k] = lanes_sum<4>(t);
+      }
+      nrm[NC - 1] = 0.f;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        L[i] = sel4(q, nrm[(4 * i) % NC], nrm[(4 * i + 1) % NC], nrm[(4 * i + 2) % NC],
+                    nrm[(4 * i + 3) % NC]);
+        R[i] = sel4(q, nrm[NC - 1 - 4 * i], nrm[NC - 2 - 4 * i], nrm[NC - 3 - 4 * i],
+                    nrm[NC - 4 - 4 * i]);
+      }
     }
-    nrm[NC - 1] = 0.f;
     bool definite = false, band = false;
 #pragma unroll U
     for (int rd = 0; rd < NC - 1; ++rd) {
@@ -305,7 +318,7 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
       }
       // reduce-scatter: across lanes q, q^2 keep the pairs whose bit 1 is
       // q's (pp = 2*b1 + {0, 1, 4, 5}), then across q, q^1 those whose bit
-      // 0 is q's: gv[i] is the inner product of pair q + 4i
+      // 0 is q's: the inner product of pair q + 4i
       float h[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -314,7 +327,7 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
         const float send = b1 ? gm[lo] : gm[lo + 2];
         h[j] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
       }
-      float cs_[2], sn_[2], ni_[2], nj_[2];
+      float cs_[2], sn_[2];
       bool need_[2];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
@@ -322,18 +335,14 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
         const float send = b0 ? h[2 * i] : h[2 * i + 1];
         const float gv = keep + __shfl_xor_sync(0xffffffffu, send, 1);
         const int po = q + 4 * i;  // the owned pair
-        const float al = sel4(q, nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2], nrm[4 * i + 3]);
-        const float be = sel4(q, nrm[NC - 1 - 4 * i], nrm[NC - 2 - 4 * i], nrm[NC - 3 - 4 * i],
-                              nrm[NC - 4 - 4 * i]);
+        const float al = L[i], be = R[i];
         const float g2 = gv * gv, ab = al * be;
         need_[i] = po >= 1 && po < NP && g2 > (kTol * kTol) * ab;
         cs_[i] = 1.f;
         sn_[i] = 0.f;
-        ni_[i] = al;
-        nj_[i] = be;
         if (need_[i]) {
           rotation(al, be, gv, g2, ab, cs_[i], sn_[i], definite, band);
-          rotated_norms(al, be, gv, cs_[i], sn_[i], ni_[i], nj_[i]);
+          rotated_norms(al, be, gv, cs_[i], sn_[i], L[i], R[i]);
         }
       }
       const unsigned m0 = __ballot_sync(0xffffffffu, need_[0]);
@@ -345,14 +354,27 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
         const int src = gbase | (pp & 3);
         const float cs = __shfl_sync(0xffffffffu, cs_[i], src);
         const float sn = __shfl_sync(0xffffffffu, sn_[i], src);
-        const float ni = __shfl_sync(0xffffffffu, ni_[i], src);
-        const float nj = __shfl_sync(0xffffffffu, nj_[i], src);
         A.rotate(pp, NC - 1 - pp, cs, sn);
-        nrm[pp] = ni;
-        nrm[NC - 1 - pp] = nj;
       }
       A.shift();
-      shift_norms<NC>(nrm);
+      // the norms follow their columns to the next round's owners: the new
+      // left member of pair p is the old left member of pair p + 1 (for the
+      // last pair, its own old right member), the new right member of pair p
+      // the old right member of pair p - 1 (for pair 1, the old left member
+      // of pair 0; for pair 0, the pad)
+      float nl[2], nr[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float vl = (q == 0) ? L[(i + 1) & 1] : L[i];
+        const float vr = (q == 3) ? (i == 0 ? 0.f : R[0]) : ((q == 0 && i == 0) ? L[0] : R[i]);
+        nl[i] = __shfl_sync(0xffffffffu, vl, up);
+        nr[i] = __shfl_sync(0xffffffffu, vr, dn);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        L[i] = (q + 4 * i == NP - 1) ? R[i] : nl[i];
+        R[i] = nr[i];
+      }
     }
     if (__any_sync(0xffffffffu, definite)) continue;
     if (!__any_sync(0xffffffffu, band)) break;
