@@ -614,8 +614,8 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
   ArpsChain* dch = mem.arr<ArpsChain>(hch.size());
   PGSVT_CK(cudaMemcpyAsync(dch, hch.data(), sizeof(ArpsChain) * hch.size(), cudaMemcpyHostToDevice, s));
   stats.h2d += sizeof(ArpsChain) * hch.size();
-  unsigned long long* counters = mem.arr<unsigned long long>(4);
-  PGSVT_CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+  unsigned long long* counters = mem.arr<unsigned long long>(5);
+  PGSVT_CK(cudaMemsetAsync(counters, 0, 5 * sizeof(unsigned long long), s));
   const double vP = probe_vp();
   const bool shared_probes = p.random_seed >= 0;
   int8_t* sp1 = nullptr;
@@ -831,10 +831,12 @@ void run_sequence(const void* X_dev, int dtype, int S, int nimg, double* Y_dev, 
     PGSVT_CK(cudaStreamWaitEvent(s, e, 0));
     cudaEventDestroy(e);
   }
-  unsigned long long cnt[4];
+  unsigned long long cnt[5];
   PGSVT_CK(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   PGSVT_CK(cudaStreamSynchronize(s));
   stats.d2h += sizeof(cnt);
+  if (cnt[4])
+    throw Fail(PGSVT_ERR_TIMEOUT, "SVD factors: a staged tile copy did not complete in time");
   stats.evals += cnt[3];
   stats.arps_exact += cnt[0];
   stats.svd_sweeps += cnt[1];
@@ -1024,8 +1026,8 @@ struct OneWindow {
     PGSVT_CK(cudaMemcpyAsync(plist, su.plist.data(), sizeof(int32_t) * g.NP, cudaMemcpyHostToDevice, s));
     d.plist = plist;
     d.cnt = mem.arr<int32_t>(C);
-    d.counters = mem.arr<unsigned long long>(4);
-    PGSVT_CK(cudaMemsetAsync(d.counters, 0, 32, s));
+    d.counters = mem.arr<unsigned long long>(5);
+    PGSVT_CK(cudaMemsetAsync(d.counters, 0, 5 * sizeof(unsigned long long), s));
     d.nchains = 2 * g.fw;
     const double vP = probe_vp();
     d.d2neg = -1 * std::sqrt((1 - vP) / vP);
@@ -1494,9 +1496,11 @@ int pgsvt_svd_window_ex(const double* u, uint32_t nrows, uint32_t nwin, uint32_t
     ow.alloc_factors(1);
     PGSVT_CK(launch_svd(ow.pb, ow.d, ow.s));
     *npatch = (uint32_t)g.NP;
-    unsigned long long c[4];
+    unsigned long long c[5];
     PGSVT_CK(cudaMemcpyAsync(c, ow.d.counters, sizeof(c), cudaMemcpyDeviceToHost, ow.s));
     PGSVT_CK(cudaStreamSynchronize(ow.s));
+    if (c[4])
+      throw Fail(PGSVT_ERR_TIMEOUT, "SVD factors: a staged tile copy did not complete in time");
     stats.svd_launches = 1;
     stats.svd_matrices = (uint64_t)g.NP;
     stats.svd_sweeps = c[1];

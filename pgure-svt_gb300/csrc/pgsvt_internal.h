@@ -192,7 +192,8 @@ struct DeviceBuffers {
   double* Y;               // output [nimg][S*S] (double)
   double* est;             // output estimates (nimg x 4)
   unsigned long long* counters;  // [0] ARPS FP64 steps, [1] SVD warp-sweeps,
-                                 // [2] FP64 convergence tests, [3] risk evaluations
+                                 // [2] FP64 convergence decisions, [3] risk
+                                 // evaluations, [4] expired staged-copy waits
   // learned lambda proposal
   const int32_t* feat_slots;  // sampled kept-patch slots of the features
   int nfeat_slots;

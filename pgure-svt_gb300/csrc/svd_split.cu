@@ -24,10 +24,21 @@
 // (the default for patch sides 2..4): k_bsweep runs the register form's
 // sweeps on B at four resident blocks per SM, k_bout the factors, exactly as
 // the single-kernel form computes them.
+#include <cuda.h>
+
+#include <cstring>
+
 #include "svd_kernel.cuh"
 
 namespace pgsvt {
 namespace svdk {
+
+// Tensor maps of the factors kernel's staged tiles: the normalised windows,
+// the risk fields of copies 0 and 1/2, and the probe codes of copies 1/2.
+struct BoutMaps {
+  CUtensorMap u, f0, f2, d2;
+};
+
 namespace {
 
 constexpr int kQL = 16;  // lanes per patch in the QR and the epilogue
@@ -88,6 +99,47 @@ __device__ __forceinline__ float half_sum(float v) {  // over the 16 lanes of a 
 #pragma unroll
   for (int o = 1; o < kQL; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// ---- TMA staging of frame tiles (k_bout<NC, true>)
+//
+// The 32 patches of a factors block are 8 x 4 neighbouring grid positions
+// (the tile order of the kept patches), so in every slice of the window their
+// trajectory positions fall in a small box.  One thread of the block loads,
+// per slice, a tile of the normalised window, of the risk field and of the
+// probe codes around that box with cp.async.bulk.tensor into the block's own
+// shared memory (one mbarrier, bounded wait); the lanes then assemble their
+// Casorati rows from shared memory.  Slices whose box does not fit a tile,
+// and blocks that straddle two windows or copies, read global memory as the
+// unstaged kernel does.  The tensor maps cover this device's buffers only.
+constexpr int kTR = 24, kTC = 12;  // fp32 tile: rows (inner, 96 bytes) x columns
+constexpr int kTRP = 32;           // probe-code tile rows (uint8, 32 bytes)
+constexpr int kTile = kTR * kTC, kPTile = kTRP * kTC;
+constexpr unsigned kSpinPolls = 1u << 22;  // bounded mbarrier polls
+
+__device__ __forceinline__ uint32_t smem_addr(const void* ptr) {
+  return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (unsigned it = 0; it < kSpinPolls; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_tile3(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];"
+      :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
 }
 
 // ---- Householder QR of every patch's Casorati matrix, X = R^T to xq
@@ -420,8 +472,9 @@ __global__ void __launch_bounds__(128, 4) k_bsweep(Problem pb, DeviceBuffers d, 
   }
 }
 
-template <int NC>
-__global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, int nitems) {
+template <int NC, bool TMA>
+__global__ void __launch_bounds__(128, 4)
+    k_bout(Problem pb, DeviceBuffers d, int nitems, const __grid_constant__ BoutMaps tm) {
   constexpr int RX = 4, XR = 16;
   const Geometry& g = pb.g;
   const int lane = threadIdx.x & 31, q = lane & 3;
@@ -467,22 +520,167 @@ __global__ void __launch_bounds__(128, 4) k_bout(Problem pb, DeviceBuffers d, in
   src.init(pb, d, p, c, w);
   // B again and, in shared memory, this lane's rows of the field G along the
   // trajectory (each lane reads back only what it wrote)
-  __shared__ __align__(16) float Gs[32][NC][4 * RX];
-  float* gs = &Gs[threadIdx.x >> 2][0][q * RX];
   float B[RX][NC];
+  float* gs;
+  if constexpr (!TMA) {
+    __shared__ __align__(16) float Gs[32][NC][4 * RX];
+    gs = &Gs[threadIdx.x >> 2][0][q * RX];
 #pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    const bool colok = live && k < nwin && nl_max > 0;
-    const size_t b = colok ? src.base(k) : 0;
+    for (int k = 0; k < NC; ++k) {
+      const bool colok = live && k < nwin && nl_max > 0;
+      const size_t b = colok ? src.base(k) : 0;
 #pragma unroll
-    for (int r = 0; r < RX; ++r) B[r][k] = (colok && roff[r] >= 0) ? src.value(b + roff[r]) : 0.f;
+      for (int r = 0; r < RX; ++r) B[r][k] = (colok && roff[r] >= 0) ? src.value(b + roff[r]) : 0.f;
+      if (fw_) {
+        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float* gp = &g4.x;
+#pragma unroll
+        for (int r = 0; r < RX; ++r)
+          if (colok && roff[r] >= 0) gp[r] = __ldg(fw_ + b + roff[r]);
+        *reinterpret_cast<float4*>(gs + k * 4 * RX) = g4;
+      }
+    }
+  } else {
+    // dynamic shared memory: [Gs (padded rows) | field tiles]; the window
+    // and probe tiles share the Gs region, which is written only after
+    // every lane has assembled B
+    constexpr int GSS = NC * 4 * RX + 16;  // Gs floats per patch (+16: no bank conflicts)
+    constexpr int GS_BYTES = 32 * GSS * 4;
+    static_assert(NC * (kTile * 4 + kPTile) <= GS_BYTES, "window tiles must fit the Gs region");
+    extern __shared__ unsigned char dyn_smem[];
+    unsigned char* sbase = (unsigned char*)(((uintptr_t)dyn_smem + 127) & ~(uintptr_t)127);
+    float* gsm = (float*)sbase;
+    float* ut = (float*)sbase;
+    uint8_t* ptl = sbase + NC * kTile * 4;
+    float* ftl = (float*)(sbase + GS_BYTES);
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int fymin[NC], fymax[NC], fxmin[NC], fxmax[NC], fy0[NC], fyp0[NC], fx0[NC];
+    __shared__ int cta_ok;
+    const int tid = threadIdx.x;
+    const uint32_t bara = smem_addr(&bar);
+    const bool probes = (c == 1 || c == 2);
+    if (tid < NC) {
+      fymin[tid] = fxmin[tid] = 0x7fffffff;
+      fymax[tid] = fxmax[tid] = -1;
+    }
+    if (tid == 0) {
+      const int g0 = blockIdx.x * 32, g1 = min(nitems, g0 + 32) - 1;
+      const int r0 = g0 / g.NP, r1 = g1 / g.NP;  // (window, copy) of the first and last item
+      cta_ok = (r0 == r1) && (r0 % d.ncopies) <= 2;
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bara), "r"(1) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // trajectory position of slice k of this patch (row | col << 16)
+    auto posk = [&](int k) -> uint32_t {
+      return (live && k < nwin) ? __ldg(src.posw + (size_t)k * src.P + src.posidx) : 0u;
+    };
+    if (cta_ok) {
+#pragma unroll 1
+      for (int k = 0; k < nwin; ++k) {
+        const uint32_t pc = posk(k);
+        const int y = (int)(pc & 0xffffu), x = (int)(pc >> 16);
+        const int ylo = __reduce_min_sync(0xffffffffu, live ? y : 0x7fffffff);
+        const int yhi = __reduce_max_sync(0xffffffffu, live ? y : -1);
+        const int xlo = __reduce_min_sync(0xffffffffu, live ? x : 0x7fffffff);
+        const int xhi = __reduce_max_sync(0xffffffffu, live ? x : -1);
+        if (lane == 0) {
+          atomicMin(&fymin[k], ylo);
+          atomicMax(&fymax[k], yhi);
+          atomicMin(&fxmin[k], xlo);
+          atomicMax(&fxmax[k], xhi);
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      unsigned bytes = 0;
+      for (int k = 0; k < NC; ++k) {
+        fy0[k] = -1;
+        if (!cta_ok || k >= nwin || fymin[k] > fymax[k]) continue;
+        const int y0 = fymin[k] & ~3, yp0 = fymin[k] & ~15, x0 = fxmin[k];
+        bool fit = fymax[k] + g.bs - y0 <= kTR && fxmax[k] + g.bs - x0 <= kTC;
+        if (probes) fit = fit && fymax[k] + g.bs - yp0 <= kTRP;
+        if (!fit) continue;
+        fy0[k] = y0;
+        fyp0[k] = yp0;
+        fx0[k] = x0;
+        bytes += kTile * 4 + (fw_ ? kTile * 4 : 0) + (probes ? kPTile : 0);
+      }
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   :: "r"(bara), "r"(bytes) : "memory");
+      const int zp = d.probe_stride ? w * nwin : 0;
+      for (int k = 0; k < NC; ++k) {
+        if (k >= nwin || fy0[k] < 0) continue;
+        tma_tile3(smem_addr(ut + k * kTile), &tm.u, fy0[k], fx0[k], w * nwin + k, bara);
+        if (fw_)
+          tma_tile3(smem_addr(ftl + k * kTile), c == 0 ? &tm.f0 : &tm.f2, fy0[k], fx0[k],
+                    w * nwin + k, bara);
+        if (probes) tma_tile3(smem_addr(ptl + k * kPTile), &tm.d2, fyp0[k], fx0[k], zp + k, bara);
+      }
+    }
+    __syncthreads();
+    const bool ok = mbar_wait(bara, 0);
+    if (__syncthreads_or(!ok)) {  // a copy did not land in time: report, drain, stop
+      if (tid == 0) atomicAdd(d.counters + 4, 1ull);
+      mbar_wait(bara, 0);
+      return;
+    }
+    // tile offsets of this lane's rows (row e of the Casorati matrix is pixel
+    // (e % bs, e / bs) of the patch)
+    int toff[RX], poff[RX];
+#pragma unroll
+    for (int r = 0; r < RX; ++r) {
+      const int e = q * RX + r;
+      toff[r] = e % g.bs + (e / g.bs) * kTR;
+      poff[r] = e % g.bs + (e / g.bs) * kTRP;
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const bool colok = live && k < nwin && nl_max > 0;
+      const uint32_t pc = colok ? posk(k) : 0u;
+      const int y = (int)(pc & 0xffffu), x = (int)(pc >> 16);
+      if (colok && fy0[k] >= 0) {
+        const float* ub = ut + k * kTile + (y - fy0[k]) + (x - fx0[k]) * kTR;
+        const uint8_t* pbs = ptl + k * kPTile + (y - fyp0[k]) + (x - fx0[k]) * kTRP;
+#pragma unroll
+        for (int r = 0; r < RX; ++r) {
+          float v = 0.f;
+          if (roff[r] >= 0) {
+            v = ub[toff[r]];
+            if (probes) v += pbs[poff[r]] ? src.pa : src.pb0;
+          }
+          B[r][k] = v;
+        }
+      } else {
+        const size_t b = colok ? (size_t)k * src.F + y + (size_t)x * src.S : 0;
+#pragma unroll
+        for (int r = 0; r < RX; ++r) B[r][k] = (colok && roff[r] >= 0) ? src.value(b + roff[r]) : 0.f;
+      }
+    }
+    __syncthreads();  // the window and probe tiles are dead: Gs takes their place
+    gs = gsm + (size_t)(threadIdx.x >> 2) * GSS + q * RX;
     if (fw_) {
-      float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      float* gp = &g4.x;
 #pragma unroll
-      for (int r = 0; r < RX; ++r)
-        if (colok && roff[r] >= 0) gp[r] = __ldg(fw_ + b + roff[r]);
-      *reinterpret_cast<float4*>(gs + k * 4 * RX) = g4;
+      for (int k = 0; k < NC; ++k) {
+        const bool colok = live && k < nwin && nl_max > 0;
+        const uint32_t pc = colok ? posk(k) : 0u;
+        const int y = (int)(pc & 0xffffu), x = (int)(pc >> 16);
+        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float* gp = &g4.x;
+        if (colok && fy0[k] >= 0) {
+          const float* fb = ftl + k * kTile + (y - fy0[k]) + (x - fx0[k]) * kTR;
+#pragma unroll
+          for (int r = 0; r < RX; ++r)
+            if (roff[r] >= 0) gp[r] = fb[toff[r]];
+        } else if (colok) {
+          const size_t b = (size_t)k * src.F + y + (size_t)x * src.S;
+#pragma unroll
+          for (int r = 0; r < RX; ++r)
+            if (roff[r] >= 0) gp[r] = __ldg(fw_ + b + roff[r]);
+        }
+        *reinterpret_cast<float4*>(gs + k * 4 * RX) = g4;
+      }
     }
   }
   int prev = -1;
@@ -559,12 +757,77 @@ cudaError_t run_svd_qr(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
 template cudaError_t run_svd_qr<10>(const Problem&, const DeviceBuffers&, cudaStream_t);
 template cudaError_t run_svd_qr<16>(const Problem&, const DeviceBuffers&, cudaStream_t);
 
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess || q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return (EncodeTiledFn)f;
+  }();
+  return fn;
+}
+
+// A 3-D map over `frames` column-major S x S frames (rows innermost) with a
+// box of box_rows x box_cols x 1; a null buffer gives an unused zero map.
+bool frame_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, const void* base, int S,
+               int frames, int box_rows, int box_cols) {
+  std::memset(m, 0, sizeof(*m));
+  if (!base) return true;
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)S, (cuuint64_t)S, (cuuint64_t)frames};
+  const cuuint64_t strides[2] = {(cuuint64_t)S * esize, (cuuint64_t)S * S * esize};
+  const cuuint32_t box[3] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, dt, 3, const_cast<void*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
 template <int NC>
 cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
   if (!d.xq || !d.xqn) return cudaErrorInvalidValue;
   const int nitems = pb.W * d.ncopies * pb.g.NP;
+  const int S = pb.g.S, nwin = pb.g.nwin;
   k_bsweep<NC><<<(nitems + 31) / 32, 128, 0, s>>>(pb, d, nitems);
-  k_bout<NC><<<(nitems + 31) / 32, 128, 0, s>>>(pb, d, nitems);
+  // the factors from shared-memory tiles staged by TMA where every map's row
+  // stride is a multiple of 16 bytes, else from global memory; the same
+  // values either way, so identical results
+  BoutMaps tm;
+  bool tma = S % 16 == 0 && d.counters != nullptr;
+  if (tma) {
+    const int pframes = d.probe_stride ? pb.W * nwin : nwin;
+    tma = frame_map(&tm.u, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, d.u, S, pb.W * nwin, kTR, kTC) &&
+          frame_map(&tm.f0, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pb.optimize ? d.fld0 : nullptr, S,
+                    pb.W * nwin, kTR, kTC) &&
+          frame_map(&tm.f2, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pb.optimize ? d.fld2 : nullptr, S,
+                    pb.W * nwin, kTR, kTC) &&
+          frame_map(&tm.d2, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, d.ncopies > 1 ? d.d2code : nullptr,
+                    S, pframes, kTRP, kTC);
+  }
+  if (tma) {
+    constexpr int GSS = NC * 16 + 16;
+    const size_t shm = (size_t)32 * GSS * 4 + (size_t)NC * kTile * 4 + 128;
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_bout<NC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (e != cudaSuccess) return e;
+    k_bout<NC, true><<<(nitems + 31) / 32, 128, shm, s>>>(pb, d, nitems, tm);
+  } else {
+    std::memset(&tm, 0, sizeof(tm));
+    k_bout<NC, false><<<(nitems + 31) / 32, 128, 0, s>>>(pb, d, nitems, tm);
+  }
   return cudaGetLastError();
 }
 
