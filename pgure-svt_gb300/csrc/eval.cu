@@ -21,6 +21,10 @@
 // deterministic.
 #include <algorithm>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "pgsvt_internal.h"
 
 namespace pgsvt {
@@ -649,18 +653,33 @@ size_t eval_smem(const Geometry& g, int nl, int& stage) {
   return base + (stage ? staged : 0);
 }
 
+// Raise, never lower, a kernel's dynamic shared-memory limit on the current
+// device.  k_eval's footprint depends on the lambda count of the round, and
+// concurrent callers (pgsvt_denoise_batch runs sequences on several host
+// threads) must not shrink the limit under another thread's launch.
+void allow_dynamic_smem(const void* kernel, size_t shm) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limit;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = limit[{dev, kernel}];
+  if (shm > cur && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)shm) == cudaSuccess)
+    cur = shm;
+}
+
 template <int BS, typename AccT>
 void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const Problem& pb,
                       const DeviceBuffers& d, int final_pass, int stage) {
   if constexpr (BS > 0 && BS * BS <= 16) {
     if (stage) {  // the left vectors staged in shared memory
-      cudaFuncSetAttribute(k_eval<BS, AccT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)shm);
+      allow_dynamic_smem((const void*)k_eval<BS, AccT, true>, shm);
       k_eval<BS, AccT, true><<<grid, threads, shm, s>>>(pb, d, final_pass);
       return;
     }
   }
-  cudaFuncSetAttribute(k_eval<BS, AccT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  allow_dynamic_smem((const void*)k_eval<BS, AccT>, shm);
   k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass);
 }
 

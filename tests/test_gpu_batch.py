@@ -199,3 +199,17 @@ def test_autotuner_picks_and_caches(capi, pkg):
     # the tuned call's outputs are those of its chosen shape
     np.testing.assert_array_equal(Y1, Y2)
     np.testing.assert_array_equal(e1, e2)
+
+
+def test_batch_workers_with_lambda_lists_of_different_sizes(capi, pkg):
+    """Sequences on concurrent workers whose rounds need different amounts
+    of shared memory (16 lambda values, then the single-lambda final pass)
+    all run: a kernel's shared-memory limit is only ever raised."""
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=23, side=64, nt=15)
+    p = capi.default_params(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s,
+                            frame_begin=7, frame_end=8)
+    seqs = [dict(X=noisy, params=p, lambdas=np.geomspace(1e-3, 100.0, 16) * (1 + 0.01 * i))
+            for i in range(8)]
+    for _ in range(3):
+        res, st = capi.denoise_batch(seqs, slots=4)
+        assert all(np.isfinite(r["risks"][7]).all() for r in res)
