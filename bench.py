@@ -59,7 +59,8 @@ def parse():
                          "frames) instead of the bench-time scaled ones")
     ap.add_argument("--autotune", type=int, default=1,
                     help="SVD kernel form: 1 tuned (default), 0 registers, 2 more lanes, "
-                    "3 shared memory, 4 eight rows per lane")
+                    "3 shared memory, 4 eight rows per lane, 5 QR-preconditioned, "
+                    "6 TMA-staged factors")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle leg (CPU baseline and parity)")
     ap.add_argument("--cpu-windows", type=int, default=16,
@@ -575,7 +576,8 @@ def main():
             "svd_sweeps_per_warp": st.svd_warp_sweeps / max(1, st.svd_matrices / 8),
             "svd_variant": {0: "registers", 1: "more lanes per patch",
                             2: "shared memory", 3: "eight rows per lane",
-                            4: "QR-preconditioned"}.get(int(st.svd_variant), "?")}
+                            4: "QR-preconditioned",
+                            5: "registers, TMA-staged factors"}.get(int(st.svd_variant), "?")}
     if not args.no_default_path:
         # the reference's default configuration (SVT() / PGURE-SVT defaults):
         # median pre-filter 5, noise parameters estimated per window, PGURE on

@@ -124,7 +124,10 @@ typedef struct {
                                its columns in shared memory; 4: 8 rows per
                                lane (patch sides <= 4 and 7..8, windows
                                <= 15); 5: the QR-preconditioned form (patch
-                               sides 5..8, windows <= 15)                    */
+                               sides 5..8, windows <= 15); 6: the two-kernel
+                               register form with the factors assembled from
+                               TMA-staged frame tiles (patch sides <= 4,
+                               windows <= 15)                                */
 } pgsvt_params;
 
 /* Optional per-frame outputs of pgsvt_denoise_ex / pgsvt_denoise_device_ex

@@ -310,7 +310,7 @@ void set_last_error(const std::string& m);
 int eval_blocks(const Geometry& g);
 int mse_blocks(const Geometry& g);
 int svd_columns(int nwin);
-constexpr int kSvdVariants = 5;
+constexpr int kSvdVariants = 6;
 int svd_variants(int M, int NC);
 bool svd_qr_form(int M, int NC);  // the QR-preconditioned SVD applies (its scratch is needed)
 int svd_default_variant(int M, int NC);

@@ -30,7 +30,7 @@ cudaError_t run_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 template <int NC>
 cudaError_t run_svd_qr(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
 template <int NC>
-cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s);
+cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s, bool tma);
 }
 
 int svd_columns(int nwin) {
@@ -55,7 +55,10 @@ bool svd_supported(int bs, int nwin) {
 // per-pair rotation arithmetic, replicated in every lane of a patch, is shared
 // by twice the rows; 2 resident blocks per SM instead of 3), variant 4
 // (patches of 17..64 rows, windows <= 15) sweeps the triangle of B's QR
-// factorisation instead of B (svd_split.cu).  For patches of at most 16 rows
+// factorisation instead of B (svd_split.cu), variant 5 is the two-kernel
+// register form with the factors kernel reading TMA-staged frame tiles
+// (svd_split.cu; measured slower than variant 0's global-memory gather, so
+// it is a candidate of the autotuner only).  For patches of at most 16 rows
 // and windows of at most 15 frames variant 0 runs its sweeps and its factors
 // in two kernels (svd_split.cu; the sweeps without the factors' registers fit
 // four resident blocks per SM instead of three), with identical results,
@@ -68,6 +71,7 @@ bool svd_variant_ok(int M, int NC, int v) {
   if (v == 1) return !(M > 16 && M <= 32);  // 5x5 patches have no variant 1
   if (v == 3) return NC <= 16 && (M <= 16 || M > 40);  // 8 x 2 and 8 x 8 lanes
   if (v == 4) return svd_qr_form(M, NC);                 // QR-preconditioned
+  if (v == 5) return M <= 16 && NC <= 16;                // two-kernel form, TMA-staged factors
   return false;
 }
 bool svd_qr_form(int M, int NC) { return M > 16 && M <= 64 && NC <= 16; }
@@ -95,9 +99,11 @@ cudaError_t launch_svd(const Problem& pb, const DeviceBuffers& d, cudaStream_t s
     if (NC == 10) return run_svd_qr<10>(pb, d, s);
     if (NC == 16) return run_svd_qr<16>(pb, d, s);
   }
-  if (pb.svd_variant == 0 && M <= 16 && d.xq && d.xqn) {  // sweeps and factors in two kernels
-    if (NC == 10) return run_svd_split<10>(pb, d, s);
-    if (NC == 16) return run_svd_split<16>(pb, d, s);
+  if ((pb.svd_variant == 0 || pb.svd_variant == 5) && M <= 16 && d.xq && d.xqn) {
+    // sweeps and factors in two kernels; variant 5 stages the factors' frame
+    // tiles with TMA
+    if (NC == 10) return run_svd_split<10>(pb, d, s, pb.svd_variant == 5);
+    if (NC == 16) return run_svd_split<16>(pb, d, s, pb.svd_variant == 5);
   }
   if (pb.svd_variant == 3 && NC <= 16) {  // 8 rows per lane
     if (M <= 16) {

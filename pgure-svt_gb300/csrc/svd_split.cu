@@ -797,16 +797,16 @@ bool frame_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, const void*
 }  // namespace
 
 template <int NC>
-cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s) {
+cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_t s, bool staged) {
   if (!d.xq || !d.xqn) return cudaErrorInvalidValue;
   const int nitems = pb.W * d.ncopies * pb.g.NP;
   const int S = pb.g.S, nwin = pb.g.nwin;
   k_bsweep<NC><<<(nitems + 31) / 32, 128, 0, s>>>(pb, d, nitems);
-  // the factors from shared-memory tiles staged by TMA where every map's row
-  // stride is a multiple of 16 bytes, else from global memory; the same
-  // values either way, so identical results
+  // the factors from shared-memory tiles staged by TMA (when asked for and
+  // every map's row stride is a multiple of 16 bytes), else from global
+  // memory; the same values either way, so identical results
   BoutMaps tm;
-  bool tma = S % 16 == 0 && d.counters != nullptr;
+  bool tma = staged && S % 16 == 0 && d.counters != nullptr;
   if (tma) {
     const int pframes = d.probe_stride ? pb.W * nwin : nwin;
     tma = frame_map(&tm.u, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, d.u, S, pb.W * nwin, kTR, kTC) &&
@@ -831,8 +831,8 @@ cudaError_t run_svd_split(const Problem& pb, const DeviceBuffers& d, cudaStream_
   return cudaGetLastError();
 }
 
-template cudaError_t run_svd_split<10>(const Problem&, const DeviceBuffers&, cudaStream_t);
-template cudaError_t run_svd_split<16>(const Problem&, const DeviceBuffers&, cudaStream_t);
+template cudaError_t run_svd_split<10>(const Problem&, const DeviceBuffers&, cudaStream_t, bool);
+template cudaError_t run_svd_split<16>(const Problem&, const DeviceBuffers&, cudaStream_t, bool);
 
 }  // namespace svdk
 }  // namespace pgsvt

@@ -213,3 +213,23 @@ def test_batch_workers_with_lambda_lists_of_different_sizes(capi, pkg):
     for _ in range(3):
         res, st = capi.denoise_batch(seqs, slots=4)
         assert all(np.isfinite(r["risks"][7]).all() for r in res)
+
+
+@pytest.mark.parametrize("side,bs,T", [(48, 4, 15), (64, 3, 7)])
+def test_tma_staged_factors_are_identical(capi, pkg, side, bs, T):
+    """The two-kernel register form with its factors kernel reading
+    TMA-staged frame tiles (variant 5, frame sides that are multiples of 16)
+    assembles the same Casorati rows and fields as the global-memory gather:
+    identical results, PGURE search included."""
+    noisy, _, (a, m, s) = pkg.synth.workload("arps_256", seed=31, side=side, nt=T + 4)
+    base = dict(median_size=0, random_seed=5, alpha=a, mu=m, sigma=s, block_size=bs,
+                traj_length=T)
+    Y0, e0, st0 = capi.denoise(noisy, capi.default_params(autotune=0, **base))
+    Y5, e5, st5 = capi.denoise(noisy, capi.default_params(autotune=6, **base))
+    assert st0.svd_variant == 0 and st5.svd_variant == 5
+    np.testing.assert_array_equal(Y5, Y0)
+    np.testing.assert_array_equal(e5, e0)
+    # fresh probes per window (negative seed: one probe set per window)
+    base["random_seed"] = -1
+    _, _, st = capi.denoise(noisy, capi.default_params(autotune=6, **base))
+    assert st.svd_variant == 5
