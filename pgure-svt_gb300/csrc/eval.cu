@@ -461,60 +461,98 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
     x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
     x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
   }
+  // Two lambda values per pass share every load of the left and right
+  // vectors (patches of at most 16 rows, whose left vectors are staged in
+  // shared memory; the larger forms keep one value per pass within their
+  // registers); each has its own half of the warp's tile.  The tile's column
+  // stride is padded to 8 (mod 32) where the footprint allows it, so that
+  // the four 8-row lane groups of a half block (one grid column each) hit
+  // disjoint banks.
   const int th = y1 - y0 + nb, tw = x1 - x0 + nb;
-  const bool use_tile = (y1 >= 0) && th * tw <= kTileMax;
+  constexpr int kHalfTile = kTileMax / 2;
+  int ths = th <= 8 ? 8 : 8 + 32 * ((th - 8 + 31) / 32);
+  if (ths * tw > kHalfTile) ths = th;
+  const bool use_tile = (y1 >= 0) && ths * tw <= kHalfTile;
   const float* U0 = d.U0 + (size_t)w * NC * M * NP;
   const float* V0 = d.V0 + (size_t)w * NC * g.nwin * NP;
   AccT* accw = (AccT*)d.acc;
   constexpr int CH = (BS > 0 && BS * BS < 16) ? BS * BS : 16;  // rows rebuilt per pass
-  for (int j = 0; j < nl; ++j) {
-    AccT* acc = accw + (((size_t)w * pb.K + j) * g.nwin + k) * g.F();
+  constexpr bool kPair = kStage;
+  for (int j0 = 0; j0 < nl; j0 += kPair ? 2 : 1) {
+    const bool two = kPair && j0 + 1 < nl;
+    AccT* acc[2];
+    int* tl[2] = {tile, tile + kHalfTile};
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj)
+      acc[jj] = accw + (((size_t)w * pb.K + (two ? j0 + jj : j0)) * g.nwin + k) * g.F();
+    const int rj = max(srmax[j0], two ? srmax[j0 + 1] : 0);
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
       if (!live[h]) continue;
       const int p = blockIdx.x * PB + h * 32 + lane;
-      const int rm = min(srmax[j], nlive[h]);
+      const int rm = min(rj, nlive[h]);
+      const float* sg0 = sg + (size_t)j0 * NC * PB + h * 32 + lane;
+      const float* sg1 = sg + (size_t)(two ? j0 + 1 : j0) * NC * PB + h * 32 + lane;
 #pragma unroll 1
       for (int e0 = 0; e0 < M; e0 += CH) {
-        float col[CH];
+        float col[2][CH];
 #pragma unroll
-        for (int e = 0; e < CH; ++e) col[e] = 0.f;
+        for (int e = 0; e < CH; ++e) col[0][e] = col[1][e] = 0.f;
         for (int i = 0; i < rm; ++i) {
-          const float coef = sg[((size_t)j * NC + i) * PB + h * 32 + lane] *
-                             V0[((size_t)i * g.nwin + k) * NP + p];
-          if (coef == 0.f) continue;
+          const float v = V0[((size_t)i * g.nwin + k) * NP + p];
+          const float c0 = sg0[(size_t)i * PB] * v;
+          const float c1 = two ? sg1[(size_t)i * PB] * v : 0.f;
+          if (c0 == 0.f && c1 == 0.f) continue;
           if constexpr (kStage) {
             const float* ui = Us + ((size_t)i * M + e0) * PB + h * 32 + lane;
 #pragma unroll
             for (int e = 0; e < CH; ++e)
-              if (e0 + e < M) col[e] = fmaf(coef, ui[e * PB], col[e]);
+              if (e0 + e < M) {
+                const float u = ui[e * PB];
+                col[0][e] = fmaf(c0, u, col[0][e]);
+                col[1][e] = fmaf(c1, u, col[1][e]);
+              }
           } else {
             const float* ui = U0 + ((size_t)i * M + e0) * NP + p;
 #pragma unroll
             for (int e = 0; e < CH; ++e)
-              if (e0 + e < M) col[e] = fmaf(coef, __ldg(ui + (size_t)e * NP), col[e]);
+              if (e0 + e < M) {
+                const float u = __ldg(ui + (size_t)e * NP);
+                col[0][e] = fmaf(c0, u, col[0][e]);
+                col[1][e] = fmaf(c1, u, col[1][e]);
+              }
           }
         }
 #pragma unroll
-        for (int e = 0; e < CH; ++e) {
-          const int ee = e0 + e;
-          const float v = col[e];
-          if (ee >= M || v == 0.f) continue;
-          const int er = ee % nb, ec = ee / nb;
-          if (use_tile && fabsf(v) <= kTileBound)
-            atomicAdd(tile + (y[h] - y0 + er) + (x[h] - x0 + ec) * th, __float2int_rn(v * 1048576.f));
-          else
-            Acc<AccT>::add(acc + (y[h] + er) + (size_t)(x[h] + ec) * g.S, Acc<AccT>::fix(v));
+        for (int jj = 0; jj < 2; ++jj) {
+          if (jj == 1 && !two) break;
+#pragma unroll
+          for (int e = 0; e < CH; ++e) {
+            const int ee = e0 + e;
+            const float val = col[jj][e];
+            if (ee >= M || val == 0.f) continue;
+            const int er = ee % nb, ec = ee / nb;
+            if (use_tile && fabsf(val) <= kTileBound)
+              atomicAdd(tl[jj] + (y[h] - y0 + er) + (x[h] - x0 + ec) * ths,
+                        __float2int_rn(val * 1048576.f));
+            else
+              Acc<AccT>::add(acc[jj] + (y[h] + er) + (size_t)(x[h] + ec) * g.S, Acc<AccT>::fix(val));
+          }
         }
       }
     }
     if (use_tile) {
       __syncwarp();
-      for (int t = lane; t < th * tw; t += 32) {
-        const int v = tile[t];
-        if (v != 0) {
-          tile[t] = 0;
-          Acc<AccT>::add(acc + (y0 + t % th) + (size_t)(x0 + t / th) * g.S, Acc<AccT>::from_tile(v));
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        if (jj == 1 && !two) break;
+        for (int t = lane; t < ths * tw; t += 32) {
+          const int v = tl[jj][t];
+          if (v != 0) {
+            tl[jj][t] = 0;
+            Acc<AccT>::add(acc[jj] + (y0 + t % ths) + (size_t)(x0 + t / ths) * g.S,
+                           Acc<AccT>::from_tile(v));
+          }
         }
       }
       __syncwarp();

@@ -86,7 +86,9 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
             gmin = float(g.min())
             c = clean[:, :, 7]
             peak = float(clean.max())
-            row = dict(grid_min=gmin, grid_argmin=float(GRID[int(np.argmin(g))]))
+            row = dict(grid_min=gmin, grid_argmin=float(GRID[int(np.argmin(g))]),
+                       proposal=float(res["learned"]["proposals"][7])
+                       if res["learned"]["proposals"] is not None else None)
             for name in ("plain", "learned"):
                 r = res[name]
                 y = r["Y"][:, :, 7]
@@ -110,6 +112,7 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
                          gap_grid_max=float(gg.max()), gap_grid_mean=float(gg.mean()),
                          frac_gap_grid_le_1pct=float(np.mean(gg <= 0.01)),
                          psnr_mean=float(col(name, "psnr").mean()))
+    out["worst_windows"] = sorted(rows, key=lambda r: -r["gap_learned_vs_plain"])[:8]
     out["psnr_delta_learned_minus_plain_db"] = dict(
         mean=float((col("learned", "psnr") - col("plain", "psnr")).mean()),
         min=float((col("learned", "psnr") - col("plain", "psnr")).min()),
