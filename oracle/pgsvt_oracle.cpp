@@ -615,10 +615,15 @@ struct SearchResult {
 // with edge = true (the narrow search's hand-over to the plain one), unless
 // that end is a bound of the search: the bottom when include_zero_lo, the
 // top when it equals `upper`.
+//
+// `sentinels` (narrow searches only): points evaluated with the round-0 grid
+// but kept out of the point list; one of them below the grid's best ends the
+// search with edge = true.
 template <typename F>
 SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t rounds,
                           double tol, uint32_t max_eval, bool include_zero_lo,
-                          double edge_flat = -1.0, double upper = -1.0) {
+                          double edge_flat = -1.0, double upper = -1.0,
+                          const std::vector<double>& sentinels = {}) {
   struct Pt { double l, r; };
   std::vector<Pt> pts;
   if (max_eval < K) K = std::max<uint32_t>(1, max_eval);
@@ -626,7 +631,9 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
     const double l = (K == 1) ? hi : lo * std::pow(hi / lo, (double)j / (double)(K - 1));
     pts.push_back({l, risk(l)});
   }
-  uint32_t evals = K;
+  double sent = std::numeric_limits<double>::infinity();
+  for (double l : sentinels) sent = std::min(sent, risk(l));
+  uint32_t evals = K + (uint32_t)sentinels.size();
   auto best_of = [&]() {
     size_t b = 0;
     for (size_t i = 1; i < pts.size(); ++i)
@@ -635,6 +642,10 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
   };
   size_t b = best_of();
   SearchResult res{pts[b].l, pts[b].r, evals, false};
+  if (sent < pts[b].r) {  // a plain-grid end does better than the narrow grid
+    res.edge = true;
+    return res;
+  }
   const bool bound = (b == 0 && include_zero_lo) || (b + 1 == pts.size() && pts[b].l >= upper &&
                                                      upper > 0.0);
   if (edge_flat >= 0.0 && (b == 0 || b + 1 == pts.size()) && !bound) {
@@ -794,9 +805,15 @@ WindowOut run_window(const double* X, const double* Z, const orc_params& p, cons
       const uint32_t Rh = p.hint_rounds ? p.hint_rounds : 1u;
       const double flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
       const double h = std::min(hint, upper);
-      const double lo = h / span;
-      sr = batch_search(rf, lo, std::min(upper, h * span), Kh, Rh, p.tol, maxe,
-                        lo <= upper * 1e-4, flat, upper);
+      const double lo = h / span, hi = std::min(upper, h * span);
+      // the plain grid's ends the narrow grid does not reach, as far as the
+      // round's size (K) and the evaluation budget leave room
+      const uint32_t kh = maxe < Kh ? std::max<uint32_t>(1, maxe) : Kh;
+      const int room = std::min((int)K - (int)kh, (int)maxe - (int)kh);
+      std::vector<double> sent;
+      if (room > 0 && lo > upper * 1e-4) sent.push_back(upper * 1e-4);
+      if (room > (int)sent.size() && hi < upper) sent.push_back(upper);
+      sr = batch_search(rf, lo, hi, Kh, Rh, p.tol, maxe, lo <= upper * 1e-4, flat, upper, sent);
       if (sr.edge) {  // proposal not bracketed: fall back to the full search
         const SearchResult full = batch_search(rf, upper * 1e-4, upper, K, R, p.tol,
                                                maxe > sr.evals ? maxe - sr.evals : 1, true);

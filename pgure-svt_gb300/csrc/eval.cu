@@ -130,6 +130,8 @@ struct Sch {
     s.evals_phase = 0;
     s.npts = 0;
     s.best = 0;
+    s.nsent = 0;
+    s.sent_risk = INFINITY;
   }
   __device__ static int best(const SearchState& s) {
     int b = 0;
@@ -142,12 +144,19 @@ struct Sch {
 // The narrow grid inherits the plain search's bounds: a grid reaching below
 // the plain grid's bottom (upper * 1e-4) may refine down to 0 as the plain
 // search does, and a grid clipped at `upper` ends there as the plain one
-// does; a best point on such a bound is a result, not a miss.
+// does; a best point on such a bound is a result, not a miss.  Its first
+// round also evaluates the plain grid's ends that it does not reach
+// (sentinels, kept out of the point list): one of them below the narrow
+// grid's best sends the search to the plain grid.
 __device__ void start_narrow(SearchState& s, const Problem& pb, double upper, double hint) {
   const double h = fmin(hint, upper);
-  const double lo = h / pb.hint_span;
+  const double lo = h / pb.hint_span, hi = fmin(upper, h * pb.hint_span);
   Sch::phase(s, 1, pb.hint_K, pb.max_evals, pb.hint_rounds, lo <= upper * 1e-4 ? 1 : 0);
-  Sch::grid(s, lo, fmin(upper, h * pb.hint_span));
+  Sch::grid(s, lo, hi);
+  const int room = min(pb.K - s.nnext, pb.max_evals - s.nnext);
+  if (room > 0 && lo > upper * 1e-4) s.next[s.nnext + s.nsent++] = upper * 1e-4;
+  if (room > s.nsent && hi < upper) s.next[s.nnext + s.nsent++] = upper;
+  s.nnext += s.nsent;
 }
 
 __global__ void k_search_init(Problem pb, DeviceBuffers d) {
@@ -163,6 +172,8 @@ __global__ void k_search_init(Problem pb, DeviceBuffers d) {
   s.final_lambda = pb.lambda_user;
   s.final_risk = 0.0;
   s.hint_lambda = s.hint_risk = 0.0;
+  s.nsent = 0;
+  s.sent_risk = INFINITY;
   if (!pb.optimize) {
     s.done = 1;
     return;
@@ -249,7 +260,8 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
   }
   if (threadIdx.x != 0) return;
   const double prev_best = s.npts > 0 ? s.risk[s.best] : 0.0;
-  for (int j = 0; j < nn; ++j) {
+  for (int j = nn - s.nsent; j < nn; ++j) s.sent_risk = fmin(s.sent_risk, risk[j]);
+  for (int j = 0; j < nn - s.nsent; ++j) {
     int pos = s.npts;  // keep lambda ascending, new points after equal ones
     while (pos > 0 && s.lam[pos - 1] > s.next[j]) {
       s.lam[pos] = s.lam[pos - 1];
@@ -275,7 +287,9 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
       const int nb = (b == 0) ? 1 : s.npts - 2;
       steep = !(s.risk[nb] - s.risk[b] <= pb.hint_flat * fabs(s.risk[b]));
     }
-    if (s.phase == 1 && steep) {  // proposal not bracketed: plain search
+    const bool beaten = s.sent_risk < s.risk[b];  // a plain-grid end does better
+    s.nsent = 0;
+    if (s.phase == 1 && (steep || beaten)) {  // proposal not bracketed: plain search
       s.hint_lambda = s.lam[b];
       s.hint_risk = s.risk[b];
       const int left = pb.max_evals > s.evals_phase ? pb.max_evals - s.evals_phase : 1;

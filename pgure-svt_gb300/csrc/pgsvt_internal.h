@@ -108,6 +108,8 @@ struct SearchState {
   double next[kMaxK];   // lambda values of the pending round
   double hint_lambda, hint_risk;
   double final_lambda, final_risk;
+  double sent_risk;     // least risk of the narrow search's sentinel points
+  int32_t nsent;        // sentinels at the end of the pending round's list
   int32_t npts, nnext, done, best;
   int32_t phase, K, max_eval, rounds, zero_lo, rd, evals_phase, evals_total, first;
 };

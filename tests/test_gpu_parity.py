@@ -422,3 +422,18 @@ def test_lambda_search_within_1pct_of_dense_grid(capi, oracle, pkg, noise):
                                        ex["evals"][t], gp, estl[t, 0], exl["evals"][t], gl))
         assert gp <= 0.01
         assert gl <= 0.01
+
+
+def test_narrow_search_sentinels_match_oracle(capi, oracle, g):
+    """A given proposal far from the risk minimum (which lies at the bottom of
+    the plain grid): GPU and oracle both see a sentinel beat the narrow grid,
+    fall back to the plain search, and spend the same evaluations."""
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    kw = dict(median_size=-1, random_seed=11, alpha=a, mu=m, sigma=s, frame_begin=6, frame_end=10,
+              lambda_hint=1.0)
+    _, est, _, ex = capi.denoise_ex(g["X"], capi.default_params(**kw))
+    _, est0, rep = oracle.denoise(g["X"], n_jobs=2, **kw)
+    f = slice(6, 10)
+    np.testing.assert_array_equal(ex["evals"][f], rep.evals[f])
+    assert np.all(ex["evals"][f] > 6)
+    np.testing.assert_allclose(est[f, 0], est0[f, 0], rtol=1e-12)

@@ -423,3 +423,17 @@ def test_q6_last_evaluation_versus_best_point(oracle):
         assert fb <= fl
         assert (fl - fb) / abs(fb) <= 1e-3
         assert (fg - fb) / abs(fb) <= 0.01
+
+
+def test_narrow_search_sentinels_send_a_misplaced_proposal_to_the_plain_grid(oracle):
+    """A proposal far from a minimum that lies at an end of the plain grid:
+    the narrow search's sentinel evaluations at the plain grid's ends beat
+    its own grid, so the plain search runs and finds the same lambda as the
+    search without a proposal."""
+    g = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])  # counts: minimum at the bottom
+    kw = dict(n_jobs=1, random_seed=11, alpha=a, mu=m, sigma=s, frame_begin=8, frame_end=9)
+    _, e_plain, r_plain = oracle.denoise(g["X"], **kw)
+    _, e_hint, r_hint = oracle.denoise(g["X"], lambda_hint=1.0, **kw)
+    assert e_hint[8, 0] == e_plain[8, 0]
+    assert r_hint.risk_evals == 4 + 2 + r_plain.risk_evals  # narrow grid, sentinels, plain search
