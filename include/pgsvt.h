@@ -107,7 +107,7 @@ typedef struct {
    * one (lambda_mlp.npz) covers 4x4 patches and 15-frame windows.          */
   const float* lambda_model;
   uint32_t hint_points;     /* lambda values per narrow-search round (0: 4) */
-  uint32_t hint_rounds;     /* refinement rounds of the narrow search (0: 1) */
+  uint32_t hint_rounds;     /* refinement rounds of the narrow search (0: 2) */
   double hint_flat;         /* a best point on the narrow grid's edge is kept
                                when its neighbour's risk is within this
                                relative amount (0: 1e-3); else the plain

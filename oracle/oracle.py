@@ -58,7 +58,7 @@ DEFAULTS = dict(traj_length=15, block_size=4, block_overlap=1, motion_window=7,
                 lambda_=-1.0, alpha=-1.0, mu=-1.0, sigma=-1.0, tol=1e-7,
                 compat_flags=COMPAT_ALL, search_points=8, search_rounds=4,
                 window_batch=0, lambda_hint=-1.0, hint_span=2.0, frame_begin=0,
-                frame_end=0, lambda_model=None, hint_points=4, hint_rounds=1, hint_flat=1e-3,
+                frame_end=0, lambda_model=None, hint_points=4, hint_rounds=2, hint_flat=1e-3,
                 autotune=0, lambda_hints=None, risk_out=None, evals_out=None,
                 window_threads=1)
 

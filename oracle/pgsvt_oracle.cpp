@@ -802,7 +802,7 @@ WindowOut run_window(const double* X, const double* Z, const orc_params& p, cons
     if (hint > 0) {
       const double span = p.hint_span > 1 ? p.hint_span : 2.0;
       const uint32_t Kh = std::min(K, p.hint_points ? p.hint_points : 4u);
-      const uint32_t Rh = p.hint_rounds ? p.hint_rounds : 1u;
+      const uint32_t Rh = p.hint_rounds ? p.hint_rounds : 2u;
       const double flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
       const double h = std::min(hint, upper);
       const double lo = h / span, hi = std::min(upper, h * span);

@@ -305,10 +305,9 @@ Setup make_setup(const pgsvt_params& p, int S, int nimg, int nfixed = 0) {
   s.rounds = p.search_rounds ? (int)p.search_rounds : 4;
   // bound the points a window keeps
   while (s.K * (1 + s.rounds) > kMaxPts && s.rounds > 0) --s.rounds;
-  // plain: 1 grid + rounds refinements; hinted: 1 + rounds/2, then possibly plain again
   // plain: 1 grid + rounds refinements; narrow (hinted or learned): 1 grid +
   // hint_rounds refinements, then possibly the plain search
-  const int hr = p.hint_rounds ? (int)p.hint_rounds : 1;
+  const int hr = p.hint_rounds ? (int)p.hint_rounds : 2;
   const bool narrow = p.lambda_hint > 0 || (p.lambda_model && p.optimize_pgure);
   s.max_rounds = narrow ? (1 + hr) + (1 + s.rounds) : 1 + s.rounds;
   if (nfixed > 0) {  // one round over a given lambda list
@@ -338,7 +337,7 @@ Problem make_problem(const pgsvt_params& p, const Setup& su) {
   pb.hint = p.lambda_hint;
   pb.hint_span = p.hint_span > 1.0 ? p.hint_span : 2.0;
   pb.hint_K = std::min(su.K, p.hint_points ? (int)p.hint_points : 4);
-  pb.hint_rounds = p.hint_rounds ? (int)p.hint_rounds : 1;
+  pb.hint_rounds = p.hint_rounds ? (int)p.hint_rounds : 2;
   pb.hint_flat = p.hint_flat > 0 ? p.hint_flat : 1e-3;
   pb.acc64 = 0;
   pb.svd_variant = svd_default_variant(pb.g.M, pb.g.NC);
@@ -1113,7 +1112,7 @@ int pgsvt_default_params(pgsvt_params* p) {
   p->frame_end = 0;
   p->lambda_model = nullptr;
   p->hint_points = 4;
-  p->hint_rounds = 1;
+  p->hint_rounds = 2;
   p->hint_flat = 1e-3;
   p->autotune = 0;
   return PGSVT_OK;

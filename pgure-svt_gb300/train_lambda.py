@@ -74,7 +74,10 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
     """Held-out 512x512x200 sequences (config 5's evaluation set): for each
     sampled window, the plain search and the learned proposal + narrow
     search, their risk against the minimum over a 256-value lambda grid (the
-    arbiter), risk evaluations and the PSNR of the denoised centre frame."""
+    arbiter), risk evaluations and the PSNR of the denoised centre frame.
+    Risk gaps are relative to the grid minimum's magnitude (gap_grid) and,
+    since a risk minimum can sit near zero, to the risk's range over the grid
+    (gap_span)."""
     L = pkg.learned
     rows = []
     mdl = np.ascontiguousarray(model, np.float32)
@@ -84,6 +87,7 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
             res = L.compare(X, noise, mdl, frames=(7, 8))
             g = grid_risks(pkg, X, noise)
             gmin = float(g.min())
+            span = float(g.max() - g.min())  # the risk's range over the grid
             c = clean[:, :, 7]
             peak = float(clean.max())
             row = dict(grid_min=gmin, grid_argmin=float(GRID[int(np.argmin(g))]),
@@ -95,6 +99,7 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
                 row[name] = dict(lam=float(r["lambdas"][7]), risk=float(r["risk"][7]),
                                  evals=int(r["evals"][7]),
                                  gap_grid=float((r["risk"][7] - gmin) / abs(gmin)),
+                                 gap_span=float((r["risk"][7] - gmin) / span) if span > 0 else 0.0,
                                  psnr=float(10 * np.log10(peak ** 2 / np.mean((c - y) ** 2))))
             rp, rl = row["plain"]["risk"], row["learned"]["risk"]
             row["gap_learned_vs_plain"] = float((rl - rp) / abs(rp))
@@ -108,9 +113,12 @@ def evaluate_512(pkg, model, seeds, pool, estimated=False):
                frac_learned_vs_plain_le_1pct=float(np.mean(gap <= 0.01)))
     for name in ("plain", "learned"):
         gg = col(name, "gap_grid")
+        gs = col(name, "gap_span")
         out[name] = dict(evals_mean=float(col(name, "evals").mean()),
                          gap_grid_max=float(gg.max()), gap_grid_mean=float(gg.mean()),
                          frac_gap_grid_le_1pct=float(np.mean(gg <= 0.01)),
+                         gap_span_max=float(gs.max()),
+                         frac_gap_span_le_1pct=float(np.mean(gs <= 0.01)),
                          psnr_mean=float(col(name, "psnr").mean()))
     out["worst_windows"] = sorted(rows, key=lambda r: -r["gap_learned_vs_plain"])[:8]
     out["psnr_delta_learned_minus_plain_db"] = dict(
