@@ -150,7 +150,9 @@ def evaluate(pkg, model, seeds, pool, estimated=False):
     gap = np.array([r["risk_gap"] for r in rows])
     return dict(windows=len(rows), rmse_log10=float(np.sqrt(np.mean((y - yh) ** 2))),
                 evals_plain=float(ep.mean()), evals_learned=float(el.mean()),
-                fallbacks=int(np.sum(el > 8)),  # beyond the narrow search's 4 + 4 values
+                # beyond the narrow search's own evaluations (grid, two
+                # sentinels, two refinement rounds of 4): the plain search ran
+                fallbacks=int(np.sum(el > 4 + 2 + 2 * 4)),
                 risk_gap_max=float(gap.max()),
                 risk_gap_mean=float(gap.mean()), frac_gap_le_1pct=float(np.mean(gap <= 0.01)))
 
