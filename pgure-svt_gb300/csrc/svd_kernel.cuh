@@ -11,6 +11,8 @@ constexpr int kMaxSweeps = 16;
 constexpr float kTol = 1e-6f;     // rotate while |a_i.a_j| > kTol |a_i| |a_j|
 constexpr float kBand = 4.f;      // near-degenerate pairs below kBand*kTol: FP64 decides
 constexpr float kDegen = 1e-3f;   // |a_i|^2 and |a_j|^2 within 0.1%: near-degenerate
+constexpr float kStopRel = 1e-3f; // owner form: a sweep whose rotations were all below
+                                  // this relative inner product is the last
 
 // Round-robin ordering with a fixed pairing pattern in register space: the
 // pad column (always zero, nwin < NC) sits at position NC-1 and meets
@@ -301,7 +303,7 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
                     nrm[NC - 4 - 4 * i]);
       }
     }
-    bool definite = false, band = false;
+    bool definite = false, band = false, big = false;
 #pragma unroll U
     for (int rd = 0; rd < NC - 1; ++rd) {
       // this lane's partial inner products of the round's pairs
@@ -342,6 +344,7 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
         sn_[i] = 0.f;
         if (need_[i]) {
           rotation(al, be, gv, g2, ab, cs_[i], sn_[i], definite, band);
+          big |= g2 > (kStopRel * kStopRel) * ab;
           rotated_norms(al, be, gv, cs_[i], sn_[i], L[i], R[i]);
         }
       }
@@ -376,7 +379,13 @@ __device__ int owner_sweeps(RegCols<4, NC>& A, float* As, int q, int nwin,
         R[i] = nr[i];
       }
     }
-    if (__any_sync(0xffffffffu, definite)) continue;
+    if (__any_sync(0xffffffffu, definite)) {
+      // every rotation of the sweep was smaller than kStopRel: convergence is
+      // quadratic, so the inner products it leaves are of order kStopRel^2,
+      // the rotation threshold, and the next sweep would be the last
+      if (!__any_sync(0xffffffffu, band) && !__any_sync(0xffffffffu, big)) break;
+      continue;
+    }
     if (!__any_sync(0xffffffffu, band)) break;
 #pragma unroll
     for (int k = 0; k < NC; ++k)
@@ -555,7 +564,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
       }
       if (q == 0) nrs[NC - 1] = 0.f;
       __syncwarp();
-      bool definite = false, band = false;
+      bool definite = false, band = false, big = false;
 #pragma unroll 1
       for (int rd = 0; rd < NC - 1; ++rd) {
         float va[NC / 2][RPL], vb[NC / 2][RPL], gm[NC / 2];
@@ -616,6 +625,7 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
             sn_[i] = 0.f;
             if (need_[i]) {
               rotation(al, be, gv, g2, ab, cs_[i], sn_[i], definite, band);
+              big |= g2 > (kStopRel * kStopRel) * ab;
               float ni, nj;
               rotated_norms(al, be, gv, cs_[i], sn_[i], ni, nj);
               nrs[ia] = ni;
@@ -673,7 +683,11 @@ __global__ void __launch_bounds__(128, (svd_minblocks<RPL, NC, SM>()))
         }
         __syncwarp();
       }
-      if (__any_sync(0xffffffffu, definite)) continue;
+      if (__any_sync(0xffffffffu, definite)) {
+        if constexpr (kOwnerForm<RPL, LANES, NC>)  // the owner form's stopping rule
+          if (!__any_sync(0xffffffffu, band) && !__any_sync(0xffffffffu, big)) break;
+        continue;
+      }
       if (!__any_sync(0xffffffffu, band)) break;
       if (!fp64_again()) break;
     }
