@@ -597,8 +597,9 @@ struct Pgure {
 // ---------------------------------------------------------------------------
 // Lambda search: bracketed batch grid search (the schedule the CUDA library
 // runs on the device).  Round 0 evaluates K points spaced geometrically over
-// [lo, hi]; each later round evaluates K points evenly inside the bracket
-// formed by the neighbours of the best point so far.  Returns the best point
+// [lo, hi]; each later round evaluates K/2 points evenly inside the bracket
+// formed by the neighbours of the best point so far (K points in a narrow
+// search, or when the bracket reaches down to zero).  Returns the best point
 // (ties: smallest lambda).  Stops early when a round improves the best risk by
 // no more than tol*|risk| while the bracket is narrower than kNarrowBracket
 // times the best point, or when max_eval is reached.
@@ -655,16 +656,21 @@ SearchResult batch_search(F&& risk, double lo, double hi, uint32_t K, uint32_t r
       return res;
     }
   }
-  for (uint32_t rd = 0; rd < rounds && evals + K <= max_eval; ++rd) {
+  for (uint32_t rd = 0; rd < rounds; ++rd) {
+    // refinement rounds of the plain search place half the grid's points,
+    // unless the bracket reaches down to the zero bound
+    const uint32_t Kr = (edge_flat >= 0.0 || (b == 0 && include_zero_lo))
+                            ? K : std::max<uint32_t>(2, K / 2);
+    if (evals + Kr > max_eval) break;
     const double blo = (b > 0) ? pts[b - 1].l : (include_zero_lo ? 0.0 : pts[b].l);
     const double bhi = (b + 1 < pts.size()) ? pts[b + 1].l : pts[b].l;
     if (!(bhi > blo)) break;
     const double prev = pts[b].r;
-    for (uint32_t i = 0; i < K; ++i) {
-      const double l = blo + (bhi - blo) * (double)(i + 1) / (double)(K + 1);
+    for (uint32_t i = 0; i < Kr; ++i) {
+      const double l = blo + (bhi - blo) * (double)(i + 1) / (double)(Kr + 1);
       pts.push_back({l, risk(l)});
     }
-    evals += K;
+    evals += Kr;
     std::stable_sort(pts.begin(), pts.end(), [](const Pt& a, const Pt& c) { return a.l < c.l; });
     b = best_of();
     res.lambda = pts[b].l;

@@ -102,8 +102,9 @@ __global__ void k_sum_u(Problem pb, DeviceBuffers d, int nblk) {
 // ---- search state machine (one thread per window)
 //
 // Bracketed batch grid search, identical to the oracle's: round 0 places K
-// points geometrically over [lo, hi]; each later round places K points evenly
-// inside the bracket formed by the neighbours of the best point so far.  A
+// points geometrically over [lo, hi]; each later round places K/2 points
+// evenly inside the bracket formed by the neighbours of the best point so far
+// (K points in a narrow search, or when the bracket reaches down to zero).  A
 // hint (a given or learned proposal) runs a narrow search first: hint_K
 // points over [hint/span, hint*span] and hint_rounds refinements.  When the
 // best point of its grid lies on an edge and the neighbouring point's risk
@@ -307,7 +308,10 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
     search_finish(s, d.counters);  // no progress and a narrow bracket
     return;
   }
-  if (s.rd >= s.rounds || s.evals_phase + s.K > s.max_eval) {
+  // refinement rounds of the plain search place half the grid's points,
+  // unless the bracket reaches down to the zero bound
+  const int Kr = (s.phase == 1 || (b == 0 && s.zero_lo)) ? s.K : max(2, s.K / 2);
+  if (s.rd >= s.rounds || s.evals_phase + Kr > s.max_eval) {
     search_finish(s, d.counters);
     return;
   }
@@ -315,9 +319,9 @@ __global__ void __launch_bounds__(256) k_search_step(Problem pb, DeviceBuffers d
     search_finish(s, d.counters);
     return;
   }
-  for (int i = 0; i < s.K; ++i)
-    s.next[i] = blo + (bhi - blo) * (double)(i + 1) / (double)(s.K + 1);
-  s.nnext = s.K;
+  for (int i = 0; i < Kr; ++i)
+    s.next[i] = blo + (bhi - blo) * (double)(i + 1) / (double)(Kr + 1);
+  s.nnext = Kr;
 }
 
 // ---- fixed-point accumulators
