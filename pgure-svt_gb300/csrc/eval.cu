@@ -483,12 +483,12 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
   // vectors (patches of at most 16 rows, whose left vectors are staged in
   // shared memory; the larger forms keep one value per pass within their
   // registers); each has its own half of the warp's tile.  The tile's column
-  // stride is padded to 8 (mod 32) where the footprint allows it, so that
-  // the four 8-row lane groups of a half block (one grid column each) hit
-  // disjoint banks.
+  // stride is padded to 8 (mod 16) where the footprint allows it, so that
+  // the four 8-row lane groups of a half block (one grid column each) start
+  // 0, 8, 16, 24 (or 0, 24, 16, 8) banks apart.
   const int th = y1 - y0 + nb, tw = x1 - x0 + nb;
   constexpr int kHalfTile = kTileMax / 2;
-  int ths = th <= 8 ? 8 : 8 + 32 * ((th - 8 + 31) / 32);
+  int ths = th <= 8 ? 8 : 8 + 16 * ((th - 8 + 15) / 16);
   if (ths * tw > kHalfTile) ths = th;
   const bool use_tile = (y1 >= 0) && ths * tw <= kHalfTile;
   const float* U0 = d.U0 + (size_t)w * NC * M * NP;
