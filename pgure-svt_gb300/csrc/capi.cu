@@ -99,8 +99,9 @@ void make_probes(int64_t seed, size_t n, int8_t* d1, int8_t* d2code) {
 std::vector<int32_t> patch_list(int S, int bs, int ov) { return kept_patches(S, bs, ov); }
 
 // Processing order of the kept patches: 8 x 8 tiles of grid positions (rows
-// fastest), so the 64 patches of a lambda-evaluation block cover a compact
-// region of every slice and their rebuilt blocks overlap (k_eval).  The
+// fastest), so the 32 patches of a lambda-evaluation block (half a tile)
+// cover a compact region of every slice and their rebuilt blocks overlap
+// (k_eval).  The
 // order has no effect on the results: the overlap sums are integer sums.
 std::vector<int32_t> tile_order(const std::vector<int32_t>& plist, int S, int bs) {
   const int n1 = S - bs + 1, ti = (n1 + 7) / 8;

@@ -347,9 +347,10 @@ struct Acc<unsigned long long> {  // 2^-32
 
 // ---- one evaluation round: shrink, linear terms, rebuild + scatter of copy 0
 //
-// Block = 64 kept patches (an 8 x 8 tile of grid positions, see the patch
-// order in capi.cu; two per lane) x nwin warps.  Phase A spreads the (lambda, copy) pairs
-// over all warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0
+// Block = 32 kept patches (an 8 x 4 half of an 8 x 8 tile of grid positions,
+// see the patch order in capi.cu; one per lane) x nwin warps, small enough
+// (about 80 KB of shared memory, 64 registers) for two blocks per SM.  Phase
+// A spreads the (lambda, copy) pairs over all warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0
 // go to shared memory and sum_i g_i h_i of every copy to per-lane partials.
 // Phase B: warp k rebuilds column k (trajectory slice k) of its lanes'
 // patches from the live singular triplets.  The 32 rebuilt blocks of one
@@ -357,23 +358,19 @@ struct Acc<unsigned long long> {  // 2^-32
 // int32 fixed point (2^-20, order-free) and adds the tile to the accumulator
 // with one atomic per touched pixel.
 
-constexpr int kTileMax = 1024;     // pixels of a warp's shared-memory tile
-constexpr float kTileBound = 30.f; // |value| above this bypasses the tile (64 x 30 < 2048)
+constexpr int kTileMax = 512;      // pixels of a warp's shared-memory tile
+constexpr float kTileBound = 60.f; // |value| above this bypasses the tile (32 x 60 < 2048)
 
-// launch bounds of k_eval (a block is 32 x nwin threads, nwin <= 21)
-#ifndef PGSVT_EVAL_THREADS
-#define PGSVT_EVAL_THREADS (32 * 21)
-#endif
-#ifndef PGSVT_EVAL_MINB
-#define PGSVT_EVAL_MINB 1
-#endif
+// launch bounds of k_eval: a block is 32 x nwin threads, nwin <= MAXW; the
+// staged forms of windows up to 16 frames run two blocks per SM
 
-template <int BS, typename AccT, bool STAGE = false>
-__global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
+template <int BS, typename AccT, bool STAGE = false, int MAXW = 21>
+__global__ void __launch_bounds__(32 * MAXW, MAXW <= 16 ? 2 : 1)
     k_eval(Problem pb, DeviceBuffers d, int final_pass) {
   const int nb = BS > 0 ? BS : pb.g.bs;  // BS == 0: any side (9..16)
   const int M = nb * nb;
   constexpr int PB = kEvalPatches;  // patches per block
+  constexpr int H = PB / 32;         // patches per lane
   const Geometry& g = pb.g;
   const int w = blockIdx.y;
   const SearchState& st = d.st[w];
@@ -395,8 +392,8 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
   if (threadIdx.x < kMaxK) srmax[threadIdx.x] = 0;
   __syncthreads();
   // phase A: (lambda, copy, half) tasks over all warps
-  for (int task = k; task < nl * ncp * 2; task += nwarps) {
-    const int h = task & 1, jc = task >> 1;
+  for (int task = k; task < nl * ncp * H; task += nwarps) {
+    const int h = task % H, jc = task / H;
     const int j = jc / ncp, c = jc % ncp;
     const int slot = h * 32 + lane;
     const int p = blockIdx.x * PB + slot;
@@ -446,18 +443,18 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
   if (lin_terms)
     for (int j = k; j < nl; j += nwarps) {
       float lin = 0.f;
-      for (int h = 0; h < 2; ++h)
+      for (int h = 0; h < H; ++h)
         for (int c = 0; c < ncp; ++c) lin += slin[((size_t)j * 4 + c) * PB + h * 32 + lane];
       const double t = warp_sum_d((double)lin);
       if (lane == 0) d.part_lin[((size_t)w * pb.K + j) * d.nblk_eval + blockIdx.x] = t;
     }
   if (k >= g.nwin) return;
   if (final_pass == 1 && k != wc.out_slice) return;  // 2: every slice
-  int y[2], x[2], nlive[2];
-  bool live[2];
+  int y[H], x[H], nlive[H];
+  bool live[H];
   int y0 = 1 << 30, y1 = -1, x0 = 1 << 30, x1 = -1;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
+  for (int h = 0; h < H; ++h) {
     const int p = blockIdx.x * PB + h * 32 + lane;
     live[h] = p < g.NP;
     y[h] = x[h] = nlive[h] = 0;
@@ -505,7 +502,7 @@ __global__ void __launch_bounds__(PGSVT_EVAL_THREADS, PGSVT_EVAL_MINB)
       acc[jj] = accw + (((size_t)w * pb.K + (two ? j0 + jj : j0)) * g.nwin + k) * g.F();
     const int rj = max(srmax[j0], two ? srmax[j0 + 1] : 0);
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
       if (!live[h]) continue;
       const int p = blockIdx.x * PB + h * 32 + lane;
       const int rm = min(rj, nlive[h]);
@@ -729,6 +726,11 @@ template <int BS, typename AccT>
 void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const Problem& pb,
                       const DeviceBuffers& d, int final_pass, int stage) {
   if constexpr (BS > 0 && BS * BS <= 16) {
+    if (stage && threads <= 32 * 16) {  // two blocks per SM
+      allow_dynamic_smem((const void*)k_eval<BS, AccT, true, 16>, shm);
+      k_eval<BS, AccT, true, 16><<<grid, threads, shm, s>>>(pb, d, final_pass);
+      return;
+    }
     if (stage) {  // the left vectors staged in shared memory
       allow_dynamic_smem((const void*)k_eval<BS, AccT, true>, shm);
       k_eval<BS, AccT, true><<<grid, threads, shm, s>>>(pb, d, final_pass);

@@ -59,7 +59,7 @@ constexpr int kMaxPts = 160;       // evaluated points kept per window
 // the point (else it refines again, within its round and evaluation limits).
 constexpr double kNarrowBracket = 0.25;
 constexpr int kMaxMW = 15;         // motion window supported by ARPS
-constexpr int kEvalPatches = 64;   // kept patches per lambda-evaluation block (8 x 8 tile)
+constexpr int kEvalPatches = 32;   // kept patches per lambda-evaluation block (8 x 4 half tile)
 constexpr double kFixScale = 4294967296.0;  // 2^32 fixed-point scale
 
 // round(v * 2^32) toward zero as an int64, with integer instructions only
