@@ -349,9 +349,10 @@ struct Acc<unsigned long long> {  // 2^-32
 //
 // Block = 32 kept patches (an 8 x 4 half of an 8 x 8 tile of grid positions,
 // see the patch order in capi.cu; one per lane) x nwin warps, small enough
-// (about 80 KB of shared memory, 64 registers) for two blocks per SM.  Phase
-// A spreads the (lambda, copy) pairs over all warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0
-// go to shared memory and sum_i g_i h_i of every copy to per-lane partials.
+// (at most about 100 KB of shared memory, 64 registers) for two blocks per
+// SM when nwin <= 16.  Phase A spreads the (lambda, copy) pairs over all
+// warps: the shrunk singular values g_i (svt.hpp:135-143) of copy 0 go to
+// shared memory and sum_i g_i h_i of every copy to per-lane partials.
 // Phase B: warp k rebuilds column k (trajectory slice k) of its lanes'
 // patches from the live singular triplets.  The 32 rebuilt blocks of one
 // slice overlap heavily, so each warp sums them into a shared-memory tile in
@@ -361,8 +362,8 @@ struct Acc<unsigned long long> {  // 2^-32
 constexpr int kTileMax = 512;      // pixels of a warp's shared-memory tile
 constexpr float kTileBound = 60.f; // |value| above this bypasses the tile (32 x 60 < 2048)
 
-// launch bounds of k_eval: a block is 32 x nwin threads, nwin <= MAXW; the
-// staged forms of windows up to 16 frames run two blocks per SM
+// launch bounds of k_eval: a block is 32 x nwin threads, nwin <= MAXW;
+// windows up to 16 frames run two blocks per SM
 
 template <int BS, typename AccT, bool STAGE = false, int MAXW = 21>
 __global__ void __launch_bounds__(32 * MAXW, MAXW <= 16 ? 2 : 1)
@@ -736,6 +737,11 @@ void launch_k_eval_bs(dim3 grid, int threads, size_t shm, cudaStream_t s, const 
       k_eval<BS, AccT, true><<<grid, threads, shm, s>>>(pb, d, final_pass);
       return;
     }
+  }
+  if (threads <= 32 * 16) {  // two blocks per SM
+    allow_dynamic_smem((const void*)k_eval<BS, AccT, false, 16>, shm);
+    k_eval<BS, AccT, false, 16><<<grid, threads, shm, s>>>(pb, d, final_pass);
+    return;
   }
   allow_dynamic_smem((const void*)k_eval<BS, AccT>, shm);
   k_eval<BS, AccT><<<grid, threads, shm, s>>>(pb, d, final_pass);
