@@ -437,3 +437,26 @@ def test_narrow_search_sentinels_send_a_misplaced_proposal_to_the_plain_grid(ora
     _, e_hint, r_hint = oracle.denoise(g["X"], lambda_hint=1.0, **kw)
     assert e_hint[8, 0] == e_plain[8, 0]
     assert r_hint.risk_evals == 4 + 2 + r_plain.risk_evals  # narrow grid, sentinels, plain search
+
+
+def test_plain_search_refinement_schedule(oracle):
+    """The plain search evaluates K = 8 grid points, then K/2 = 4 per
+    refinement round while its bracket lies inside (0, upper], and K per
+    round while the bracket reaches down to the zero bound (raw counts on the
+    normalised window: the risk falls toward lambda = 0)."""
+    g = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    X = g["X"].astype(np.float64)
+    kw = dict(n_jobs=2, random_seed=11, frame_begin=4, frame_end=12)
+    a, m, s = (float(g[k]) / X.max() for k in ("alpha", "mu", "sigma"))
+    _, est, rep = oracle.denoise(X, alpha=a, mu=m, sigma=s, **kw)
+    ev = rep.evals[4:12].astype(int)
+    print("interior optimum: lambdas", est[4:12, 0], "evaluations", ev)
+    assert np.all(est[4:12, 0] > 0)
+    assert np.all((ev - 8) % 4 == 0) and np.all(ev > 8)
+    assert np.all(ev <= 8 + 4 * 4)  # four rounds of 4 points at most
+    a, m, s = float(g["alpha"]), float(g["mu"]), float(g["sigma"])
+    _, est0, rep0 = oracle.denoise(X, alpha=a, mu=m, sigma=s, **kw)
+    ev0 = rep0.evals[4:12].astype(int)
+    print("optimum at the bottom: lambdas", est0[4:12, 0], "evaluations", ev0)
+    assert np.all((ev0 - 8) % 8 == 0) and np.all(ev0 > 8)
+    assert np.any(ev0 > 8 + 4 * 4)  # rounds of 8 points
