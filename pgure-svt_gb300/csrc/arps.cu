@@ -415,8 +415,9 @@ __device__ void arps_pair(const ArpsCtx& c, bool live, int it, int& my, int& mx,
   ox = x;
 }
 
+// five blocks per SM: 96 registers, no spills (128 at the default bound)
 template <int BS>
-__global__ void __launch_bounds__(128) k_arps(Problem pb, DeviceBuffers d) {
+__global__ void __launch_bounds__(128, 5) k_arps(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
   const int it0 = blockIdx.x * blockDim.x + threadIdx.x;
   const int ch = blockIdx.y, w = blockIdx.z;
