@@ -93,7 +93,7 @@ typedef struct {
   double sigma;             /* sigmaEst                                 */
   double tol;               /* tol (ftol of the lambda search)          */
   uint32_t compat_flags;    /* PGSVT_COMPAT_* (default PGSVT_COMPAT_ALL)*/
-  uint32_t search_points;   /* lambda values per search round (0: 8)    */
+  uint32_t search_points;   /* grid points; K/2 per refinement (0: 8)   */
   uint32_t search_rounds;   /* refinement rounds after the grid (0: 4)  */
   uint32_t window_batch;    /* windows in flight on the device (0: auto)*/
   double lambda_hint;       /* >0: narrow search around this proposal   */
