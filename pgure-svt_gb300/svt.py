@@ -24,7 +24,8 @@ class SVT:
     compat_flags : int, default=COMPAT_ALL
         Reference behaviours reproduced for parity (see include/pgsvt.h).
     search_points, search_rounds : int
-        Lambda values per search round and refinement rounds.
+        Lambda values of the search grid (each refinement round places half
+        as many) and refinement rounds.
     lambda_hint : float or None
         A proposed lambda (e.g. from the learned proposal): the search
         brackets it first and falls back to the full search.
