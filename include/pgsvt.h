@@ -373,7 +373,9 @@ int pgsvt_hot_pixel_filter(uint16_t* frames, uint32_t nrows, uint32_t ncols, uin
  * singular values, never a fault.  All calls share the array and it keeps the
  * previous call's contents: calls whose GPU work overlaps race, so serialise
  * them.  Runs on `stream` (a cudaStream_t, NULL: default stream) and returns
- * once the work has completed.  Calls no allocating routine.                */
+ * once the work has completed: it copies the patch list from pageable host
+ * memory and synchronises the stream, so no call can be captured into a
+ * CUDA graph.  Calls no allocating routine.                                  */
 #define PGSVT_NOALLOC_MAX_SIDE 64
 #define PGSVT_NOALLOC_MAX_NWIN 15
 int pgsvt_svd_window_noalloc(const float* u_dev, uint32_t nrows, uint32_t nwin,
