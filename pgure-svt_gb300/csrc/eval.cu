@@ -37,16 +37,50 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // ---- coverage counts (weights in svt.hpp:157-159)
-__global__ void k_counts(Problem pb, DeviceBuffers d) {
+//
+// A warp's 32 patches are half of an 8 x 8 tile of grid positions (the
+// processing order), so their blocks in slice k overlap: the warp counts them
+// in a shared-memory tile and adds the tile with one global atomic per
+// touched pixel (plain global atomics when the footprint does not fit).
+constexpr int kCountTile = 512;
+
+__global__ void __launch_bounds__(128) k_counts(Problem pb, DeviceBuffers d) {
   const Geometry& g = pb.g;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y, w = blockIdx.z;
-  if (p >= g.NP) return;
-  const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
-  const int y = pc & 0xffffu, x = pc >> 16;
+  const int lane = threadIdx.x & 31;
+  __shared__ int tiles[4][kCountTile];
+  int* tile = tiles[threadIdx.x >> 5];
+  const bool live = p < g.NP;
+  int y = 0, x = 0;
+  if (live) {
+    const uint32_t pc = d.pos[((size_t)w * g.nwin + k) * g.P + d.plist[p]];
+    y = pc & 0xffffu;
+    x = pc >> 16;
+  }
+  const int y0 = __reduce_min_sync(0xffffffffu, live ? y : 0x7fffffff);
+  const int y1 = __reduce_max_sync(0xffffffffu, live ? y : -1);
+  const int x0 = __reduce_min_sync(0xffffffffu, live ? x : 0x7fffffff);
+  const int x1 = __reduce_max_sync(0xffffffffu, live ? x : -1);
+  if (y1 < 0) return;  // no live patch in this warp (warp-uniform)
   int32_t* c = d.cnt + (size_t)w * g.cube() + (size_t)k * g.F();
-  for (int cc = 0; cc < g.bs; ++cc)
-    for (int r = 0; r < g.bs; ++r) atomicAdd(c + (y + r) + (size_t)(x + cc) * g.S, 1);
+  const int th = y1 - y0 + g.bs, tw = x1 - x0 + g.bs;
+  if (th * tw > kCountTile) {  // warp-uniform
+    if (live)
+      for (int cc = 0; cc < g.bs; ++cc)
+        for (int r = 0; r < g.bs; ++r) atomicAdd(c + (y + r) + (size_t)(x + cc) * g.S, 1);
+    return;
+  }
+  for (int i = lane; i < th * tw; i += 32) tile[i] = 0;
+  __syncwarp();
+  if (live)
+    for (int cc = 0; cc < g.bs; ++cc)
+      for (int r = 0; r < g.bs; ++r) atomicAdd(tile + (y - y0 + r) + (x - x0 + cc) * th, 1);
+  __syncwarp();
+  for (int i = lane; i < th * tw; i += 32) {
+    const int v = tile[i];
+    if (v) atomicAdd(c + (y0 + i % th) + (size_t)(x0 + i / th) * g.S, v);
+  }
 }
 
 // ---- lambda-independent fields and sum(U)
