@@ -516,8 +516,8 @@ __global__ void __launch_bounds__(32 * MAXW, MAXW <= 16 ? 2 : 1)
   // shared memory; the larger forms keep one value per pass within their
   // registers); each has its own half of the warp's tile.  The tile's column
   // stride is padded to 8 (mod 16) where the footprint allows it, so that
-  // the four 8-row lane groups of a half block (one grid column each) start
-  // 0, 8, 16, 24 (or 0, 24, 16, 8) banks apart.
+  // the warp's four 8-row lane groups (one grid column each) start 0, 8, 16,
+  // 24 (or 0, 24, 16, 8) banks apart.
   const int th = y1 - y0 + nb, tw = x1 - x0 + nb;
   constexpr int kHalfTile = kTileMax / 2;
   int ths = th <= 8 ? 8 : 8 + 16 * ((th - 8 + 15) / 16);
